@@ -1,0 +1,394 @@
+#!/usr/bin/env python
+"""Benchmark of the splat pipeline: 1080p frames/s at 6M splats.
+
+Workload ("6M splats, SH degree 3, clustered, 1920x1080, 128-pose fly-through"): 6M seeded splats
+(64 Gaussian clusters + 20% background in a 40^3 box, SH degree 3), rendered at 1920x1080 with
+fovy 60 deg along a seeded 128-pose fly-through whose views cull part of the scene and put the near
+plane through clusters.  Synthetic data (no public dataset).  A step is one frame at the next pose.
+The resident scene (1.4 GB) is larger than L2, so there is no L2 flush between frames.
+
+Arms:
+  default            the GB300 path (libsplatter_cuda.so through the C ABI); prints one JSON line
+  --impl reference   the reference's CPU path (its CPU depth-sort fallback, renderer.rs:372-395,
+                     plus the restated vertex/fragment/blend of shaders.wgsl) on the host cores,
+                     from the oracle's C restatement: the reference itself (Rust + wgpu) cannot be
+                     built or run here
+
+Multi-GPU: a frame does not shard (depth order is global), so --gpus N runs N independent replicas
+(one rank per GPU, no collective on the data path); value = frames of all ranks / max rank time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "1080p frames/s @6M splats"
+WORKLOAD = "6M splats, SH degree 3, clustered 40^3 box, 1920x1080, fovy 60, 128-pose fly-through"
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--splats", type=int, default=6_000_000)
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--poses", type=int, default=128)
+    p.add_argument("--seed", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU-baseline sample budget")
+    p.add_argument("--out", default=None, help="also write the JSON line to this file")
+    return p.parse_args(argv)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu_index), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------------
+def workload(args):
+    import numpy as np
+    from splatter_gb300 import camera, synthetic
+    rec = synthetic.clustered(args.splats, seed=args.seed, sh_order=3)
+    poses = camera.flythrough_poses(args.poses, seed=args.seed + 7)
+    return rec, [np.asarray(p, np.float32) for p in poses]
+
+
+def config_for(args):
+    from splatter_gb300 import BlendMode, Configuration, DepthSorting
+    return Configuration(depth_sorting=DepthSorting.GPU, use_covariance_for_scale=True, use_unaligned_rectangles=True,
+                         spherical_harmonics_order=3, max_splat_count=args.splats,
+                         field_of_view_y=math.radians(60.0), blend_mode=BlendMode.UNORM8)
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-stage DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        try:
+            return json.load(open(path))
+        except Exception:
+            return {}
+    return {}
+
+
+def stage_bytes(stage, V, D, P, N, W, H, sh_order=3):
+    """Algorithmic DRAM bytes of one launch of a stage (per-unit figures x units processed)."""
+    shb = 12 * (sh_order + 1) ** 2
+    if stage == "cull":
+        return 12 * N + 8 * V                       # x,y,z read; (key, index) written per visible splat
+    if stage == "preprocess":
+        return (4 + 12 + 16 + 16 + shb + 64) * V    # index, centre, rotation, scale+alpha, SH; 64-B record
+    if stage == "depth_sort":
+        return (12 + 3 * 16) * V                    # 4 passes: read key(+value), write key+value
+    if stage == "bin":
+        return (4 + 8) * D + 8 * P                  # order + box words per drawn entry; (tile, slot) pairs
+    if stage == "pair_sort":
+        return 2 * 16 * P                           # 2 passes over 8-byte pairs
+    if stage == "ranges":
+        return 4 * P + 8 * ((W + 15) // 16) * ((H + 15) // 16)
+    if stage == "raster":
+        return (4 + 48) * P + 4 * W * H             # slot + 48-B record per pair, RGBA8 image write
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from splatter_gb300 import Renderer, Scene
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    from splatter_gb300 import build as b
+    b.build()
+
+    rec, poses = workload(args)
+    W, H = args.width, args.height
+    cfg = config_for(args)
+    r = Renderer(cfg)
+    s = Scene(r, args.splats)
+    s.load_chunk(rec)
+    r.reserve(W, H)
+    stream = torch.cuda.current_stream()
+    out = r.output_buffer(W, H)
+    torch.cuda.synchronize()
+
+    def frame(k):
+        r.render_frame(s, poses[k % len(poses)], W, H, out=out, stream=stream)
+
+    # ---- device-timed frames (inputs resident in HBM) ----
+    for k in range(args.warmup):
+        frame(k)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    visible = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    gpu_index = int(visible.split(",")[dev]) if visible and visible.split(",")[dev].strip().isdigit() else dev
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        frame(args.warmup + k)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_total = t_start.elapsed_time(t_end)
+    if world > 1:
+        tt = torch.tensor([ms_total], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(tt.item())
+        torch.distributed.barrier()
+    ms_per_step = ms_total / args.steps
+    value = world * args.steps / (ms_total / 1000.0)
+
+    # ---- per-stage timing (CUDA events on the launching streams), same frames ----
+    r.set_profiling(True)
+    stage_ms = {}
+    stage_bytes_sum = {}
+    vis_tot = 0
+    frames_prof = min(args.steps, len(poses))
+    for k in range(frames_prof):
+        frame(args.warmup + k)
+        st = r.stage_times()
+        info = r.frame_info()
+        vis_tot += info.visible_count
+        for name, ms in st.items():
+            stage_ms[name] = stage_ms.get(name, 0.0) + ms
+            stage_bytes_sum[name] = stage_bytes_sum.get(name, 0) + stage_bytes(
+                name, info.visible_count, info.draw_count, info.pair_count, args.splats, W, H)
+    r.set_profiling(False)
+    peak, peak_kind = load_peaks()
+    stages = {}
+    for name in stage_ms:
+        if name == "frame":
+            continue
+        avg_ms = stage_ms[name] / frames_prof
+        gbs = stage_bytes_sum[name] / (stage_ms[name] / 1000.0) / 1e9 if stage_ms[name] > 0 else 0.0
+        stages[name] = {"ms": round(avg_ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
+    dominant = max(stages, key=lambda n: stages[n]["ms"])
+    traffic = load_traffic().get(dominant)
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": stages[dominant]["gbs"], "peak": peak,
+                "unit": "GB/s", "frac": stages[dominant]["frac"], "peak_kind": f"{peak_kind} hbm_gbs",
+                "traffic": traffic, "algorithmic_bytes_per_launch": int(stage_bytes_sum[dominant] / frames_prof)}
+
+    # ---- end to end through the public API with host buffers ----
+    host = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
+    cam_host = [np.ascontiguousarray(p) for p in poses]
+    torch.cuda.synchronize()
+    e2e_frames = args.steps
+    t0 = time.perf_counter()
+    for k in range(e2e_frames):
+        r.render_frame(s, cam_host[(args.warmup + k) % len(poses)], W, H, out=out, stream=stream)
+        host.copy_(out, non_blocking=True)
+        stream.synchronize()
+    t1 = time.perf_counter()
+    e2e_ms = (t1 - t0) * 1000.0
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    e2e = {"value": round(world * e2e_frames / (e2e_ms / 1000.0), 2), "unit": "frames/s",
+           "h2d_bytes_per_step": 64, "d2h_bytes_per_step": W * H * 4,
+           "note": "spl_render_frame via ctypes (camera matrix from host memory) + RGBA8 image to pinned host, "
+                   "synchronised every frame"}
+
+    launches = r.launches_per_frame(W, H) * args.steps
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, rec, poses, budget_s=args.cpu_budget_s)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered splats)",
+            "config": {"workload": WORKLOAD, "splats": args.splats, "width": W, "height": H,
+                       "sh_order": 3, "depth_sorting": "Gpu", "blend": "unorm8", "poses": args.poses,
+                       "mean_visible": int(vis_tot / frames_prof), "l2": "inputs (1.4 GB scene) larger than L2",
+                       "parallelism": f"replicas x{world}"},
+            "splats_per_s": round(value * args.splats, 0),
+            "stages": stages, "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        s_line = json.dumps(line)
+        print(s_line, flush=True)
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(s_line + "\n")
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(args, rec, poses, budget_s=20.0, threads=None):
+    """The reference's CPU path (oracle port) on a bounded sample of the workload."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    sc = oracle.load_transform(rec)
+    cfg = oracle.config_struct(depth_sorting=1, sh_order=3, use_covariance_for_scale=True,
+                               use_unaligned_rectangles=True, blend_mode=0)
+    t_sort = t_vert = t_rast = 0.0
+    frames = 0
+    stride = 1
+    t_begin = time.perf_counter()
+    k = 0
+    while True:
+        u = oracle.uniforms(poses[k % len(poses)], args.width, args.height, fovy=math.radians(60.0))
+        _, v, secs = oracle.cpu_frame_timed(u, cfg, sc, threads=threads, tile_stride=stride)
+        if k == 0 and secs[2] > 5.0:
+            stride = int(math.ceil(secs[2] / 5.0))  # later frames rasterise every stride-th tile
+            k += 1
+            continue
+        t_sort += secs[0]
+        t_vert += secs[1]
+        t_rast += secs[2] * stride
+        frames += 1
+        k += 1
+        if time.perf_counter() - t_begin > budget_s or frames >= len(poses):
+            break
+    per_frame = (t_sort + t_vert + t_rast) / frames
+    return {"value": round(1.0 / per_frame, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{frames} frame(s) of the workload; CPU depth-sort fallback single-threaded, vertex stage "
+                      f"and raster on {threads} threads" + (f", raster timed on every {stride}th tile and scaled"
+                                                            if stride > 1 else ""),
+            "seconds_per_frame": {"sort": round(t_sort / frames, 3), "vertex": round(t_vert / frames, 3),
+                                  "raster": round(t_rast / frames, 3)}}
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    rec, poses = workload(args)
+    import oracle
+    threads = os.cpu_count() or 1
+    sc = oracle.load_transform(rec)
+    cfg = oracle.config_struct(depth_sorting=1, sh_order=3, use_covariance_for_scale=True,
+                               use_unaligned_rectangles=True, blend_mode=0)
+    # size the per-step sample so that the whole run stays within a few minutes
+    u = oracle.uniforms(poses[0], args.width, args.height, fovy=math.radians(60.0))
+    _, _, secs = oracle.cpu_frame_timed(u, cfg, sc, threads=threads)
+    full = sum(secs)
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    stride = 1 if full <= budget else int(math.ceil(secs[2] / max(budget - secs[0] - secs[1], 0.05)))
+    for k in range(args.warmup):
+        u = oracle.uniforms(poses[k % len(poses)], args.width, args.height, fovy=math.radians(60.0))
+        oracle.cpu_frame_timed(u, cfg, sc, threads=threads, tile_stride=stride)
+    tot = 0.0
+    for k in range(args.steps):
+        u = oracle.uniforms(poses[(args.warmup + k) % len(poses)], args.width, args.height, fovy=math.radians(60.0))
+        _, _, secs = oracle.cpu_frame_timed(u, cfg, sc, threads=threads, tile_stride=stride)
+        tot += secs[0] + secs[1] + secs[2] * stride
+    value = args.steps / tot
+    sample = (f"each step one frame of the workload: CPU depth-sort fallback (1 thread, renderer.rs:372-395) + "
+              f"restated vertex/fragment/blend on {threads} threads"
+              + (f"; raster timed on every {stride}th 16x16 tile and scaled" if stride > 1 else ""))
+    line = {"metric": METRIC, "value": round(value, 4), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * tot / args.steps, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered splats)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "splats": args.splats, "width": args.width, "height": args.height},
+            "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference (Rust + wgpu 0.17) cannot be built here and no graphics stack exists; its CPU "
+                    "path is timed through the oracle's C restatement"}
+    s_line = json.dumps(line)
+    print(s_line, flush=True)
+    if args.out:
+        with open(args.out, "w") as f:
+            f.write(s_line + "\n")
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

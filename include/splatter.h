@@ -1,0 +1,205 @@
+/*
+ * splatter.h — C ABI of libsplatter_cuda.so, the GB300 (sm_103a) implementation of splatter's
+ * per-frame splat pipeline (Lichtso/splatter: src/renderer.rs, src/scene.rs, src/shaders.wgsl).
+ *
+ * The entry points mirror the reference's Rust API one to one; each declaration names the Rust item
+ * it replaces (file:line in the reference).  Plain C types only: device buffers are raw pointers,
+ * CUDA streams are passed as `void*` (a cudaStream_t; NULL = the legacy default stream), so a Rust
+ * crate can bind this header with `extern "C"` + `#[repr(C)]` without CUDA headers.
+ *
+ * Errors: every call that can fail returns an SPL_* status (the reference panics via unwrap/assert);
+ * spl_last_error_string() describes the last failure of the calling thread.  No C++ exception
+ * crosses this boundary.
+ *
+ * Ownership and threading (renderer.rs:64-84, scene.rs:35-41): the caller owns every handle and
+ * frees it with the matching *_destroy.  A renderer owns its sorting/binning scratch, so it renders
+ * one frame at a time (calls on one renderer must not overlap on the GPU).  A scene may be rendered
+ * by several renderers that were created on the same device.
+ */
+#ifndef SPLATTER_H
+#define SPLATTER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SPL_API __attribute__((visibility("default")))
+#else
+#define SPL_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------------ */
+#define SPL_OK 0
+#define SPL_ERR_INVALID 1          /* bad argument or configuration (reference: assert, renderer.rs:90) */
+#define SPL_ERR_OOM 2              /* device or pinned allocation failed */
+#define SPL_ERR_IO 3               /* file could not be read or parsed (reference: unwrap, scene.rs:202-224) */
+#define SPL_ERR_LOOKBACK_TIMEOUT 4 /* a bounded decoupled look-back wait ran out (no hang, no trap) */
+#define SPL_ERR_CUDA 5             /* a CUDA runtime call failed */
+#define SPL_ERR_CAPACITY 6         /* the tile-binning pair list overflowed max_pair_count */
+
+/* ---- configuration (renderer.rs:14-47) ----------------------------------------------------------- */
+/* DepthSorting (renderer.rs:14-23). */
+#define SPL_DEPTH_SORTING_NONE 0
+#define SPL_DEPTH_SORTING_CPU 1
+#define SPL_DEPTH_SORTING_GPU 2
+#define SPL_DEPTH_SORTING_GPU_INDIRECT_DRAW 3
+
+/* Blend target (extension): the reference blends into a Bgra8Unorm surface
+ * (application_framework.rs:184); UNORM8 reproduces that with per-blend re-quantisation and writes
+ * RGBA8 (A = final transmittance, i.e. the destination alpha the reference leaves behind).  FP32
+ * blends in f32 and writes float4 (r, g, b, T). */
+#define SPL_BLEND_UNORM8 0
+#define SPL_BLEND_FP32 1
+
+/* Configuration (renderer.rs:26-47) minus `surface_configuration` (no surface: output is a device
+ * buffer), plus three documented extensions at the end. */
+typedef struct spl_config {
+    int32_t depth_sorting;              /* renderer.rs:29-30 */
+    int32_t use_covariance_for_scale;   /* renderer.rs:31-32 (bool) */
+    int32_t use_unaligned_rectangles;   /* renderer.rs:33-34 (bool) */
+    uint32_t spherical_harmonics_order; /* renderer.rs:35-36, 0..=3 */
+    uint64_t max_splat_count;           /* renderer.rs:37-38, 1 .. 2^30-1 */
+    uint32_t radix_bits_per_digit;      /* renderer.rs:39-40, must divide 32 (renderer.rs:89-90); the
+                                           device sort always ranks 8 bits per pass — the order is
+                                           the same stable order for every valid value */
+    float frustum_culling_tolerance;    /* renderer.rs:41-42 */
+    float ellipse_margin;               /* renderer.rs:43-44 */
+    float splat_scale;                  /* renderer.rs:45-46 */
+    float field_of_view_y;              /* extension: the reference hard-codes pi/2 (renderer.rs:366) */
+    int32_t blend_mode;                 /* extension: SPL_BLEND_* */
+    uint64_t max_pair_count;            /* extension: capacity of the (tile, splat) list; 0 = 16 x
+                                           max_splat_count (at least 2^20), at most 2^30-1 */
+} spl_config;
+
+typedef struct spl_renderer spl_renderer; /* Renderer, renderer.rs:64-84 */
+typedef struct spl_scene spl_scene;       /* Scene, scene.rs:35-41 */
+
+/* Counters of the last frame a renderer rendered (read back after the frame completes). */
+typedef struct spl_frame_info {
+    uint64_t splat_count;   /* N of the scene */
+    uint64_t visible_count; /* V: splats inside the frustum (sorted / compacted entries) */
+    uint64_t draw_count;    /* entries drawn: DrawIndirect.instance_count in GpuIndirectDraw mode
+                               (shaders.wgsl:458-461); keys != 0xFFFFFFFF in Gpu mode; V otherwise */
+    uint64_t pair_count;    /* (tile, splat) pairs the binning produced (may exceed capacity) */
+    uint32_t device_error;  /* raw device error bits (1 = look-back timeout, 2 = pair overflow) */
+    uint32_t width, height;
+} spl_frame_info;
+
+/* The `Configuration` literal of the reference's viewer (showcase.rs:39-50), with max_splat_count
+ * 4Mi, field_of_view_y = pi/2 (the reference's fixed value), blend_mode UNORM8. */
+SPL_API void spl_config_default(spl_config* cfg);
+
+/* ---- renderer (renderer.rs:86-352) ---------------------------------------------------------------- */
+/* Renderer::new (renderer.rs:88): validates the configuration (radix bits must divide 32,
+ * renderer.rs:89-90) and allocates the sorting and binning scratch on the current CUDA device. */
+SPL_API int spl_renderer_create(const spl_config* cfg, spl_renderer** out);
+SPL_API void spl_renderer_destroy(spl_renderer* r);
+/* Sizes the per-resolution scratch for frames up to width x height, so that later frames of that
+ * size neither allocate nor synchronise (required before capturing render_frame into a CUDA graph). */
+SPL_API int spl_renderer_reserve(spl_renderer* r, uint32_t width, uint32_t height);
+
+/* Renderer::render_frame (renderer.rs:355-466): renders `scene` seen from `camera_to_world` (16
+ * floats, column-major: right, up, forward, position — what motor3d_to_mat4 of the camera motor
+ * gives, utils.rs:31-42) into `out_device` (width*height RGBA8 for SPL_BLEND_UNORM8, float4 for
+ * SPL_BLEND_FP32, row-major, top row first).  Asynchronous on `stream`, like queue.submit
+ * (renderer.rs:465); call spl_renderer_frame_info to wait and read the frame's counters/status. */
+SPL_API int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
+                     uint32_t height, void* out_device, void* stream);
+
+/* Waits for the renderer's last frame and returns its counters; returns SPL_ERR_LOOKBACK_TIMEOUT or
+ * SPL_ERR_CAPACITY when the device flagged one. */
+SPL_API int spl_renderer_frame_info(spl_renderer* r, spl_frame_info* info);
+
+/* Copies the last frame's visible entries — (depth key, splat index) in draw order: stable-sorted by
+ * key for the sorting modes, index order for None — into device arrays of `capacity` entries (the
+ * reference's debug readback of the entry buffer, renderer.rs:462-464).  Asynchronous on `stream`. */
+SPL_API int spl_renderer_copy_entries(spl_renderer* r, uint32_t* keys_device, uint32_t* indices_device, uint64_t capacity,
+                              void* stream);
+
+/* Copies the last frame's per-splat screen-space records (16 floats per visible splat, in compaction
+ * order = ascending splat index) into a device array of `capacity` records.  Asynchronous. */
+SPL_API int spl_renderer_copy_records(spl_renderer* r, float* records_device, uint64_t capacity, void* stream);
+
+/* Host math of render_frame (renderer.rs:364-409, utils.rs:45-70): the 224-byte uniform block for a
+ * camera and viewport.  No GPU work. */
+SPL_API int spl_compute_uniforms(const spl_config* cfg, const float camera_to_world[16], uint32_t width, uint32_t height,
+                         void* uniforms_out_224);
+
+/* ---- scene (scene.rs:43-264) ------------------------------------------------------------------ */
+/* Scene::new (scene.rs:45): allocates resident SoA splat arrays for min(splat_count, max_splat_count)
+ * splats (scene.rs:46); *clamped_count receives that number (may be NULL). */
+SPL_API int spl_scene_create(spl_renderer* r, uint64_t splat_count, spl_scene** out, uint64_t* clamped_count);
+SPL_API void spl_scene_destroy(spl_scene* s);
+SPL_API uint64_t spl_scene_splat_count(const spl_scene* s);
+/* Bytes of device memory the scene's arrays occupy (236 per splat). */
+SPL_API uint64_t spl_scene_device_bytes(const spl_scene* s);
+
+/* Scene::new_dev_test (scene.rs:158-192): three splats on the unit axes. */
+SPL_API int spl_scene_create_dev_test(spl_renderer* r, spl_scene** out);
+
+/* Scene::parse_file_header (scene.rs:197-213): header length in bytes and `element vertex` count.
+ * The reference keeps the header length in a u16 (scene.rs:211); here it is a u32. */
+SPL_API int spl_parse_file_header(const char* path, uint32_t* header_bytes, uint64_t* splat_count);
+
+/* Scene::load_chunk (scene.rs:216-264) from host memory: `count` records of 62 floats (248 bytes,
+ * scene.rs:15-24) for splats [start, start+count) (clamped to the scene, scene.rs:217).  The
+ * records are staged through pinned memory and copied with cudaMemcpyAsync; the transform (rotor
+ * normalisation, clamped exp of the log-scales, sigmoid opacity, SH copy) runs on the device.  The
+ * host buffer may be reused when the call returns; the device work is asynchronous on `stream`. */
+SPL_API int spl_scene_load_chunk(spl_scene* s, const void* records, uint64_t start, uint64_t count, void* stream);
+
+/* Scene::load_chunk reading the records straight from a splat file (seek to header + start*248,
+ * scene.rs:220-224) into the pinned staging buffers. */
+SPL_API int spl_scene_load_chunk_file(spl_scene* s, const char* path, uint32_t header_bytes, uint64_t start, uint64_t count,
+                              void* stream);
+
+/* Writes splats already in the reference's device layout (60 floats: rotation[4], centre[3], pad,
+ * scale[3], alpha, colourSH[48]; scene.rs:32, shaders.wgsl:28-35) from host memory — the write
+ * new_dev_test does (scene.rs:178-182). */
+SPL_API int spl_scene_write_splats(spl_scene* s, const float* splats60, uint64_t start, uint64_t count, void* stream);
+
+/* Reads splats back in the same 60-float layout into host memory (synchronous). */
+SPL_API int spl_scene_read_splats(const spl_scene* s, float* splats60, uint64_t start, uint64_t count);
+
+/* ---- device sort (radixSortB/radixSortC, shaders.wgsl:338-498) --------------------------------- */
+/* Stable LSD onesweep sort of `count` (key, value) pairs on the device: keys_in/values_in are
+ * sorted into keys_out/values_out by the low `key_bits` bits of the key (8, 16, 24 or 32).
+ * Uses the renderer's scratch (count <= max_splat_count).  Asynchronous on `stream`. */
+SPL_API int spl_sort_pairs(spl_renderer* r, const uint32_t* keys_in, const uint32_t* values_in, uint32_t* keys_out,
+                   uint32_t* values_out, uint64_t count, uint32_t key_bits, void* stream);
+
+/* ---- diagnostics ----------------------------------------------------------------------------------- */
+/* Stage timing with CUDA events on the launching streams (off by default).  When enabled, each
+ * render_frame records events around its stages; spl_renderer_stage_times waits for the last frame
+ * and writes SPL_STAGE_COUNT durations in milliseconds, indexed by SPL_STAGE_*.  The vertex stage
+ * runs on a side stream and overlaps the depth sort, so the stage times may sum to more than the
+ * frame time. */
+#define SPL_STAGE_CULL 0       /* cull + key + histogram + compaction */
+#define SPL_STAGE_PREPROCESS 1 /* vertex stage: colour, conic, rectangle records */
+#define SPL_STAGE_DEPTH_SORT 2 /* four onesweep passes over the visible keys */
+#define SPL_STAGE_BIN 3        /* tile binning */
+#define SPL_STAGE_PAIR_SORT 4  /* onesweep passes over the tile ids */
+#define SPL_STAGE_RANGES 5     /* per-tile list ranges */
+#define SPL_STAGE_RASTER 6     /* tile raster + blend */
+#define SPL_STAGE_FRAME 7      /* whole frame on the main stream */
+#define SPL_STAGE_COUNT 8
+SPL_API int spl_renderer_set_profiling(spl_renderer* r, int enable);
+SPL_API int spl_renderer_stage_times(spl_renderer* r, float* milliseconds, int count);
+/* Number of kernel launches (plus memsets) one render_frame issues with this configuration at this
+ * viewport. */
+SPL_API int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint32_t height);
+
+SPL_API const char* spl_last_error_string(void);
+/* Runs one bounded look-back wait against a predecessor that never publishes, with a wait limit of
+ * `spin_limit` polls, and reports whether the kernel returned with the timeout flag set
+ * (*timed_out = 1).  Used to check that waits end with an error status instead of hanging. */
+SPL_API int spl_debug_lookback_timeout(uint32_t spin_limit, int* timed_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPLATTER_H */

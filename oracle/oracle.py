@@ -1,0 +1,198 @@
+"""ctypes wrapper around oracle/_build/liboracle.so (TEST INFRASTRUCTURE ONLY).
+
+Each function cites the reference code it restates (Lichtso/splatter).  Arrays are numpy, SoA:
+centers (N,3) f32, rotations (N,4) f32 (scalar first), scales (N,3) f32, alphas (N,) f32,
+sh (N,48) f32 with coefficient k of channel c at column 3k+c (shaders.wgsl:268-294).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+__all__ = [
+    "lib", "uniforms", "cull_keys", "draw_list", "preprocess", "raster", "render", "load_transform",
+    "cpu_sort_fallback", "cpu_frame_timed", "expf", "OCFG", "UNIFORM_DTYPE", "config_struct",
+]
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        u64 = ctypes.c_uint64
+        L.oracle_expf.restype = ctypes.c_float
+        L.oracle_expf.argtypes = [ctypes.c_float]
+        L.oracle_uniforms.restype = None
+        L.oracle_uniforms.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_float, P]
+        L.oracle_cull_keys.restype = None
+        L.oracle_cull_keys.argtypes = [P, ctypes.c_int, P, u64, P, P]
+        L.oracle_draw_list.restype = None
+        L.oracle_draw_list.argtypes = [P, ctypes.c_int, P, u64, P, P, P, P]
+        for name in ("oracle_preprocess_f32", "oracle_preprocess_f64"):
+            f = getattr(L, name)
+            f.restype = u64
+            f.argtypes = [P, P, P, P, P, P, P, P, u64, P, P, ctypes.c_int]
+        L.oracle_raster.restype = None
+        L.oracle_raster.argtypes = [P, P, P, u64, P, ctypes.c_int]
+        L.oracle_render.restype = u64
+        L.oracle_render.argtypes = [P, P, P, P, P, P, P, u64, P, ctypes.c_int, P]
+        L.oracle_load_transform.restype = None
+        L.oracle_load_transform.argtypes = [P, u64, P, P, P, P, P]
+        L.oracle_cpu_sort_fallback.restype = u64
+        L.oracle_cpu_sort_fallback.argtypes = [P, P, u64, P]
+        L.oracle_cpu_frame_timed.restype = u64
+        L.oracle_cpu_frame_timed.argtypes = [P, P, P, P, P, P, P, u64, P, ctypes.c_int, ctypes.c_int, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+# 224-byte uniform block (renderer.rs:49-61).
+UNIFORM_DTYPE = np.dtype([
+    ("camera", "<f4", 16), ("view", "<f4", 16), ("vp", "<f4", 16), ("view_size", "<f4", 2),
+    ("image_size", "<u4", 2), ("tol", "<f4"), ("bias", "<f4"), ("margin", "<f4"), ("splat_scale", "<f4"),
+])
+assert UNIFORM_DTYPE.itemsize == 224
+
+OCFG = np.dtype([("depth_sorting", "<i4"), ("use_covariance_for_scale", "<i4"),
+                 ("use_unaligned_rectangles", "<i4"), ("sh_order", "<i4"), ("blend_mode", "<i4")])
+
+
+def config_struct(depth_sorting=2, use_covariance_for_scale=True, use_unaligned_rectangles=True, sh_order=3,
+                  blend_mode=0):
+    c = np.zeros(1, OCFG)
+    c["depth_sorting"] = int(depth_sorting)
+    c["use_covariance_for_scale"] = int(bool(use_covariance_for_scale))
+    c["use_unaligned_rectangles"] = int(bool(use_unaligned_rectangles))
+    c["sh_order"] = int(sh_order)
+    c["blend_mode"] = int(blend_mode)
+    return c
+
+
+def expf(x):
+    return lib().oracle_expf(float(x))
+
+
+def uniforms(cam_to_world, width, height, fovy=np.pi / 2, tol=1.1, margin=2.0, splat_scale=1.0):
+    """Frame uniforms (renderer.rs:364-409, utils.rs:45-70); cam_to_world is (4,4) column-major
+    flattened to 16 floats (columns: right, up, forward, position)."""
+    cam = _c(np.asarray(cam_to_world, np.float32).reshape(16), np.float32)
+    u = np.zeros(1, UNIFORM_DTYPE)
+    lib().oracle_uniforms(_p(cam), int(width), int(height), float(fovy), float(tol), float(margin),
+                          float(splat_scale), _p(u))
+    return u
+
+
+def cull_keys(u, mode, centers):
+    """Per-splat key and visibility (shaders.wgsl:318-324 or renderer.rs:372-392 for mode 1)."""
+    c = _c(centers, np.float32)
+    n = c.shape[0]
+    keys = np.empty(n, np.uint32)
+    vis = np.empty(n, np.uint8)
+    lib().oracle_cull_keys(_p(u), int(mode), _p(c), n, _p(keys), _p(vis))
+    return keys, vis.astype(bool)
+
+
+def draw_list(u, mode, centers):
+    """Ordered visible entries (key, index), V and draw count for a depth-sorting mode."""
+    c = _c(centers, np.float32)
+    n = c.shape[0]
+    keys = np.empty(max(n, 1), np.uint32)
+    idx = np.empty(max(n, 1), np.uint32)
+    nv = np.zeros(1, np.uint64)
+    nd = np.zeros(1, np.uint64)
+    lib().oracle_draw_list(_p(u), int(mode), _p(c), n, _p(keys), _p(idx), _p(nv), _p(nd))
+    v = int(nv[0])
+    return keys[:v].copy(), idx[:v].copy(), v, int(nd[0])
+
+
+def preprocess(u, cfg, scene, idx, fp64=False, threads=8):
+    """Vertex-stage restatement (shaders.wgsl:507-573) for splat indices idx.
+
+    Returns (records (n,16) f32, dbg (n,18) = M[9] t[2] rot[2] axes[2] rgb[3], n_valid)."""
+    centers, rots, scales, alphas, shs = (_c(scene[k], np.float32) for k in ("center", "rotation", "scale",
+                                                                            "alpha", "sh"))
+    idx = _c(idx, np.uint32)
+    n = idx.shape[0]
+    recs = np.empty((max(n, 1), 16), np.float32)
+    dbg = np.empty((max(n, 1), 18), np.float64 if fp64 else np.float32)
+    f = lib().oracle_preprocess_f64 if fp64 else lib().oracle_preprocess_f32
+    nvalid = f(_p(u), _p(cfg), _p(centers), _p(rots), _p(scales), _p(alphas), _p(shs), _p(idx), n, _p(recs),
+               _p(dbg), int(threads))
+    return recs[:n], dbg[:n], int(nvalid)
+
+
+def raster(u, cfg, records, threads=8):
+    W, H = (int(x) for x in u["image_size"][0])
+    recs = _c(records, np.float32).reshape(-1, 16)
+    if int(cfg["blend_mode"][0]) == 0:
+        out = np.zeros((H, W, 4), np.uint8)
+    else:
+        out = np.zeros((H, W, 4), np.float32)
+    lib().oracle_raster(_p(u), _p(cfg), _p(recs), recs.shape[0], _p(out), int(threads))
+    return out
+
+
+def render(u, cfg, scene, threads=8):
+    """Whole frame through the restated pipeline; returns (image, (V, n_draw, n_valid))."""
+    centers, rots, scales, alphas, shs = (_c(scene[k], np.float32) for k in ("center", "rotation", "scale",
+                                                                            "alpha", "sh"))
+    W, H = (int(x) for x in u["image_size"][0])
+    if int(cfg["blend_mode"][0]) == 0:
+        out = np.zeros((H, W, 4), np.uint8)
+    else:
+        out = np.zeros((H, W, 4), np.float32)
+    stats = np.zeros(3, np.uint64)
+    lib().oracle_render(_p(u), _p(cfg), _p(centers), _p(rots), _p(scales), _p(alphas), _p(shs),
+                        centers.shape[0], _p(out), int(threads), _p(stats))
+    return out, tuple(int(s) for s in stats)
+
+
+def load_transform(records):
+    """Scene::load_chunk transform (scene.rs:225-250) of (N,62) f32 PLY records into SoA arrays."""
+    r = _c(records, np.float32).reshape(-1, 62)
+    n = r.shape[0]
+    out = {
+        "center": np.empty((n, 3), np.float32), "rotation": np.empty((n, 4), np.float32),
+        "scale": np.empty((n, 3), np.float32), "alpha": np.empty(n, np.float32),
+        "sh": np.empty((n, 48), np.float32),
+    }
+    lib().oracle_load_transform(_p(r), n, _p(out["center"]), _p(out["rotation"]), _p(out["scale"]),
+                                _p(out["alpha"]), _p(out["sh"]))
+    return out
+
+
+def cpu_frame_timed(u, cfg, scene, threads=8, tile_stride=1):
+    """The reference's CPU path for one frame (CPU depth-sort fallback + restated vertex/fragment/blend),
+    timed per stage; returns (image, V, (t_sort, t_vertex, t_raster) seconds)."""
+    centers, rots, scales, alphas, shs = (_c(scene[k], np.float32) for k in ("center", "rotation", "scale",
+                                                                            "alpha", "sh"))
+    W, H = (int(x) for x in u["image_size"][0])
+    out = np.zeros((H, W, 4), np.uint8 if int(cfg["blend_mode"][0]) == 0 else np.float32)
+    secs = np.zeros(3, np.float64)
+    v = lib().oracle_cpu_frame_timed(_p(u), _p(cfg), _p(centers), _p(rots), _p(scales), _p(alphas), _p(shs),
+                                     centers.shape[0], _p(out), int(threads), int(tile_stride), _p(secs))
+    return out, int(v), tuple(float(x) for x in secs)
+
+
+def cpu_sort_fallback(u, positions):
+    """The reference's CPU depth-sort fallback (renderer.rs:372-395): (V,2) u32 entries (key, index)."""
+    p = _c(positions, np.float32)
+    n = p.shape[0]
+    ent = np.empty((max(n, 1), 2), np.uint32)
+    v = lib().oracle_cpu_sort_fallback(_p(u), _p(p), n, _p(ent))
+    return ent[:v]

@@ -1,0 +1,10 @@
+"""splatter_gb300: GB300-native (sm_103a) implementation of splatter's per-frame splat pipeline.
+
+The compute path is libsplatter_cuda.so (hand-written CUDA behind the C ABI in include/splatter.h);
+this package is its Python host mirror of the reference's Renderer/Scene API.
+"""
+from .renderer import (BlendMode, Configuration, DepthSorting, FrameInfo, Renderer, Scene, SplatterError,
+                       compute_uniforms)
+
+__all__ = ["BlendMode", "Configuration", "DepthSorting", "FrameInfo", "Renderer", "Scene", "SplatterError",
+           "compute_uniforms"]

@@ -1,0 +1,807 @@
+// Host runtime and C ABI of libsplatter_cuda.so (declared in include/splatter.h).
+//
+// Mirrors the reference's host side (Lichtso/splatter src/renderer.rs, src/scene.rs, src/utils.rs):
+// Renderer owns the per-frame scratch (the reference's sorting buffer, entry buffers A/B and uniform
+// buffer, renderer.rs:292-331), Scene owns resident splat arrays (scene.rs:45-155).  Instead of
+// bind groups and compute/render passes, render_frame launches the sm_103a kernels on a CUDA stream;
+// every per-frame size lives in device memory, so a frame never synchronises with the host and can
+// be captured into a CUDA graph.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "../../include/splatter.h"
+#include "spl_types.h"
+
+using namespace spl;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(SPL_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                      \
+    } while (0)
+
+constexpr uint64_t MAX_COUNT = (1ull << 30) - 1;  // look-back status words carry 30-bit counts
+constexpr uint32_t DEFAULT_SPIN_LIMIT = 1u << 20;
+constexpr uint64_t CHUNK_RECORDS = 1u << 16;  // staging ring piece (16.25 MB of 248-byte records)
+
+template <typename T>
+int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return SPL_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(SPL_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    }
+    return SPL_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+// Frame uniforms (renderer.rs:364-409; utils.rs:45-70).  The camera is the camera-to-world matrix
+// (motor3d_to_mat4 of the motor, utils.rs:31-42); the view matrix is its rigid inverse (the
+// reference inverts the motor, renderer.rs:365).  field_of_view_y is a documented extension (the
+// reference fixes pi/2, renderer.rs:366); view_width = aspect * view_height equals the reference's
+// aspect / view_height there, because view_height == 1.
+static void compute_uniforms(const spl_config& cfg, const float* cam, uint32_t W, uint32_t H, Uniforms& u) {
+    std::memcpy(u.camera, cam, 64);
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) u.view[c * 4 + r] = cam[r * 4 + c];
+    for (int r = 0; r < 3; ++r)
+        u.view[12 + r] = -((cam[r * 4 + 0] * cam[12] + cam[r * 4 + 1] * cam[13]) + cam[r * 4 + 2] * cam[14]);
+    u.view[3] = 0.0f;
+    u.view[7] = 0.0f;
+    u.view[11] = 0.0f;
+    u.view[15] = 1.0f;
+    const float half = cfg.field_of_view_y * 0.5f;
+    const float vh = (float)std::tan((double)half);
+    const float aspect = (float)W / (float)H;
+    const float vw = aspect * vh;
+    const float nearp = 1.0f, farp = 1000.0f;
+    const float den = 1.0f / (nearp - farp);
+    // perspective_projection (utils.rs:45-55), columns
+    const float P[16] = {1.0f / vw, 0, 0, 0, 0, 1.0f / vh, 0, 0, 0, 0, -farp * den, 1.0f, 0, 0, nearp * farp * den, 0};
+    // mat4_multiplication (utils.rs:58-65): column i = sum_k P[k] * V[i][k], in k order
+    for (int i = 0; i < 4; ++i)
+        for (int r = 0; r < 4; ++r)
+            u.vp[i * 4 + r] = ((P[0 * 4 + r] * u.view[i * 4 + 0] + P[1 * 4 + r] * u.view[i * 4 + 1]) +
+                               P[2 * 4 + r] * u.view[i * 4 + 2]) +
+                              P[3 * 4 + r] * u.view[i * 4 + 3];
+    u.view_size[0] = vw;
+    u.view_size[1] = vh;
+    u.image_size[0] = W;
+    u.image_size[1] = H;
+    u.tol = cfg.frustum_culling_tolerance;
+    u.bias = (0.2f * vw) / (float)W;  // renderer.rs:404
+    u.margin = cfg.ellipse_margin;
+    u.splat_scale = cfg.splat_scale;
+}
+
+struct spl_renderer {
+    spl_config cfg{};
+    int device = 0;
+    uint64_t max_n = 0;
+    uint64_t pair_cap = 0;
+    uint32_t spin_limit = DEFAULT_SPIN_LIMIT;
+    // depth sort: K1 writes keys_a/idx; 4 passes a->b->a->b->a leave (key, slot) in keys_a/vals_a
+    uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr, *idx = nullptr;
+    float4* rec = nullptr;
+    uint64_t* st_cull = nullptr;  // [ceil(max_n/4096)]
+    uint64_t* st_sort = nullptr;  // [4][ceil(max_n/4096) * 256]
+    uint64_t* st_bin = nullptr;   // [ceil(max_n/1024)]
+    uint32_t *pk_a = nullptr, *pk_b = nullptr, *pv_a = nullptr, *pv_b = nullptr;
+    uint64_t* st_pairs = nullptr;  // [3][ceil(pair_cap/4096) * 256]
+    FrameCounters* fc = nullptr;
+    FrameCounters* fc_sort = nullptr;  // counters of spl_sort_pairs
+    uint32_t* epoch = nullptr;
+    FrameCounters* host_fc = nullptr;  // pinned
+    uint2* ranges = nullptr;
+    uint64_t ranges_cap = 0;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // last frame
+    cudaStream_t last_stream = nullptr;
+    bool has_frame = false;
+    uint32_t last_w = 0, last_h = 0;
+    uint64_t last_n = 0;
+    const uint32_t* final_pair_vals = nullptr;
+    // stage profiling: events 0..8 on the main stream, 9..10 on the side stream
+    bool profiling = false;
+    cudaEvent_t ev_prof[11] = {};
+
+    uint64_t sort_tiles() const { return ceil_div(max_n, SORT_TILE); }
+    uint64_t pair_tiles() const { return ceil_div(pair_cap, SORT_TILE); }
+
+    void release() {
+        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec);
+        dfree(st_cull); dfree(st_sort); dfree(st_bin);
+        dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b); dfree(st_pairs);
+        dfree(fc); dfree(fc_sort); dfree(epoch); dfree(ranges);
+        if (host_fc) cudaFreeHost(host_fc);
+        host_fc = nullptr;
+        if (aux) cudaStreamDestroy(aux);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        aux = nullptr;
+        ev_fork = ev_join = nullptr;
+        for (auto& e : ev_prof) {
+            if (e) cudaEventDestroy(e);
+            e = nullptr;
+        }
+    }
+    void mark(int i, cudaStream_t s) {
+        if (profiling) cudaEventRecord(ev_prof[i], s);
+    }
+};
+
+struct Staging {
+    float* pinned[2] = {nullptr, nullptr};
+    float* dev[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int next = 0;
+};
+
+struct spl_scene {
+    spl_renderer* renderer = nullptr;
+    int device = 0;
+    uint64_t n = 0;
+    float *x = nullptr, *y = nullptr, *z = nullptr, *sh = nullptr;
+    float4 *rot = nullptr, *scale_alpha = nullptr;
+    Staging stg;
+    std::mutex stg_mu;
+
+    SceneView view() const { return SceneView{x, y, z, rot, scale_alpha, sh, (uint32_t)n}; }
+    void release() {
+        dfree(x); dfree(y); dfree(z); dfree(sh); dfree(rot); dfree(scale_alpha);
+        for (int i = 0; i < 2; ++i) {
+            if (stg.pinned[i]) cudaFreeHost(stg.pinned[i]);
+            dfree(stg.dev[i]);
+            if (stg.ev[i]) cudaEventDestroy(stg.ev[i]);
+            stg.pinned[i] = nullptr;
+            stg.ev[i] = nullptr;
+        }
+    }
+};
+
+static int validate_config(const spl_config* c) {
+    if (!c) return fail(SPL_ERR_INVALID, "config is NULL");
+    if (c->depth_sorting < 0 || c->depth_sorting > 3) return fail(SPL_ERR_INVALID, "depth_sorting %d", c->depth_sorting);
+    if (c->spherical_harmonics_order > 3)
+        return fail(SPL_ERR_INVALID, "spherical_harmonics_order %u > 3", c->spherical_harmonics_order);
+    const uint32_t b = c->radix_bits_per_digit;
+    if (b == 0 || b > 32 || 32 % b != 0)  // renderer.rs:89-90
+        return fail(SPL_ERR_INVALID, "radix_bits_per_digit %u does not divide 32", b);
+    if (c->max_splat_count == 0 || c->max_splat_count > MAX_COUNT)
+        return fail(SPL_ERR_INVALID, "max_splat_count %llu outside [1, 2^30-1]", (unsigned long long)c->max_splat_count);
+    if (c->blend_mode != SPL_BLEND_UNORM8 && c->blend_mode != SPL_BLEND_FP32)
+        return fail(SPL_ERR_INVALID, "blend_mode %d", c->blend_mode);
+    if (!(c->field_of_view_y > 0.0f && c->field_of_view_y < 3.14159265f))
+        return fail(SPL_ERR_INVALID, "field_of_view_y %f outside (0, pi)", (double)c->field_of_view_y);
+    if (!std::isfinite(c->frustum_culling_tolerance) || !std::isfinite(c->ellipse_margin) ||
+        !std::isfinite(c->splat_scale))
+        return fail(SPL_ERR_INVALID, "non-finite configuration value");
+    if (c->max_pair_count > MAX_COUNT) return fail(SPL_ERR_INVALID, "max_pair_count above 2^30-1");
+    return SPL_OK;
+}
+
+static int ensure_ranges(spl_renderer* r, uint64_t tiles) {
+    if (tiles <= r->ranges_cap) return SPL_OK;
+    cudaError_t e = cudaDeviceSynchronize();  // the old buffer may still be read by a frame in flight
+    if (e != cudaSuccess) return fail(SPL_ERR_CUDA, "ranges resize: %s", cudaGetErrorString(e));
+    dfree(r->ranges);
+    r->ranges_cap = 0;
+    int rc = dalloc(&r->ranges, tiles);
+    if (rc) return rc;
+    r->ranges_cap = tiles;
+    return SPL_OK;
+}
+
+static int ensure_staging(spl_scene* s) {
+    for (int i = 0; i < 2; ++i) {
+        if (!s->stg.pinned[i]) {
+            cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&s->stg.pinned[i]), CHUNK_RECORDS * 62 * 4);
+            if (e != cudaSuccess) {
+                s->stg.pinned[i] = nullptr;
+                return fail(SPL_ERR_OOM, "pinned staging: %s", cudaGetErrorString(e));
+            }
+        }
+        if (!s->stg.dev[i]) {
+            int rc = dalloc(&s->stg.dev[i], CHUNK_RECORDS * 62);
+            if (rc) return rc;
+        }
+        if (!s->stg.ev[i]) {
+            cudaError_t e = cudaEventCreateWithFlags(&s->stg.ev[i], cudaEventDisableTiming);
+            if (e != cudaSuccess) return fail(SPL_ERR_CUDA, "event: %s", cudaGetErrorString(e));
+        }
+    }
+    return SPL_OK;
+}
+
+// Shared staging loop: fill(pinned, first, count) puts `count` items of `item_floats` floats into the
+// pinned buffer; the items are copied to the device and converted by `convert`.
+template <typename Fill, typename Convert>
+static int staged_upload(spl_scene* s, uint64_t start, uint64_t count, size_t item_floats, cudaStream_t st, Fill fill,
+                         Convert convert) {
+    std::lock_guard<std::mutex> lk(s->stg_mu);
+    int rc = ensure_staging(s);
+    if (rc) return rc;
+    uint64_t done = 0;
+    while (done < count) {
+        const uint64_t cnt = (count - done) < CHUNK_RECORDS ? (count - done) : CHUNK_RECORDS;
+        const int slot = s->stg.next;
+        s->stg.next ^= 1;
+        CU(cudaEventSynchronize(s->stg.ev[slot]));
+        rc = fill(s->stg.pinned[slot], start + done, cnt);
+        if (rc) return rc;
+        CU(cudaMemcpyAsync(s->stg.dev[slot], s->stg.pinned[slot], cnt * item_floats * 4, cudaMemcpyHostToDevice, st));
+        convert(s->stg.dev[slot], start + done, cnt, st);
+        CU(cudaGetLastError());
+        CU(cudaEventRecord(s->stg.ev[slot], st));
+        done += cnt;
+    }
+    return SPL_OK;
+}
+
+extern "C" {
+
+void spl_config_default(spl_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->depth_sorting = SPL_DEPTH_SORTING_GPU;  // showcase.rs:41
+    cfg->use_covariance_for_scale = 1;           // showcase.rs:42
+    cfg->use_unaligned_rectangles = 1;           // showcase.rs:43
+    cfg->spherical_harmonics_order = 2;          // showcase.rs:44
+    cfg->max_splat_count = 1024ull * 1024 * 4;   // showcase.rs:45
+    cfg->radix_bits_per_digit = 8;               // showcase.rs:46
+    cfg->frustum_culling_tolerance = 1.1f;       // showcase.rs:47
+    cfg->ellipse_margin = 2.0f;                  // showcase.rs:48
+    cfg->splat_scale = 1.0f;                     // showcase.rs:49
+    cfg->field_of_view_y = 1.57079632679489661923f;  // renderer.rs:366
+    cfg->blend_mode = SPL_BLEND_UNORM8;
+    cfg->max_pair_count = 0;
+}
+
+const char* spl_last_error_string(void) { return g_err.c_str(); }
+
+int spl_compute_uniforms(const spl_config* cfg, const float camera_to_world[16], uint32_t width, uint32_t height,
+                         void* out) {
+    int rc = validate_config(cfg);
+    if (rc) return rc;
+    if (!camera_to_world || !out || width == 0 || height == 0) return fail(SPL_ERR_INVALID, "bad uniform arguments");
+    Uniforms u;
+    compute_uniforms(*cfg, camera_to_world, width, height, u);
+    std::memcpy(out, &u, sizeof(u));
+    return SPL_OK;
+}
+
+int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
+    if (!out) return fail(SPL_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int rc = validate_config(cfg);
+    if (rc) return rc;
+    spl_renderer* r = new (std::nothrow) spl_renderer();
+    if (!r) return fail(SPL_ERR_OOM, "host allocation failed");
+    r->cfg = *cfg;
+    cudaGetDevice(&r->device);
+    r->max_n = cfg->max_splat_count;
+    uint64_t pc = cfg->max_pair_count;
+    if (pc == 0) {
+        pc = r->max_n * 16;
+        if (pc < (1ull << 20)) pc = 1ull << 20;
+        if (pc > MAX_COUNT) pc = MAX_COUNT;
+    }
+    r->pair_cap = pc;
+    const uint64_t n = r->max_n;
+    const uint64_t st_sort_words = 4 * r->sort_tiles() * 256;
+    const uint64_t st_pair_words = 3 * r->pair_tiles() * 256;
+#define TRY(x)           \
+    do {                 \
+        rc = (x);        \
+        if (rc) {        \
+            r->release(); \
+            delete r;    \
+            return rc;   \
+        }                \
+    } while (0)
+    TRY(dalloc(&r->keys_a, n));
+    TRY(dalloc(&r->keys_b, n));
+    TRY(dalloc(&r->vals_a, n));
+    TRY(dalloc(&r->vals_b, n));
+    TRY(dalloc(&r->idx, n));
+    TRY(dalloc(&r->rec, n * 4));
+    TRY(dalloc(&r->st_cull, ceil_div(n, CULL_TILE)));
+    TRY(dalloc(&r->st_sort, st_sort_words));
+    TRY(dalloc(&r->st_bin, ceil_div(n, BIN_TILE)));
+    TRY(dalloc(&r->pk_a, pc));
+    TRY(dalloc(&r->pk_b, pc));
+    TRY(dalloc(&r->pv_a, pc));
+    TRY(dalloc(&r->pv_b, pc));
+    TRY(dalloc(&r->st_pairs, st_pair_words));
+    TRY(dalloc(&r->fc, 1));
+    TRY(dalloc(&r->fc_sort, 1));
+    TRY(dalloc(&r->epoch, 1));
+#undef TRY
+    cudaError_t e = cudaSuccess;
+    // status words start at epoch 0, which no frame uses
+    if (e == cudaSuccess) e = cudaMemset(r->st_cull, 0, ceil_div(n, CULL_TILE) * 8);
+    if (e == cudaSuccess) e = cudaMemset(r->st_sort, 0, st_sort_words * 8);
+    if (e == cudaSuccess) e = cudaMemset(r->st_bin, 0, ceil_div(n, BIN_TILE) * 8);
+    if (e == cudaSuccess) e = cudaMemset(r->st_pairs, 0, st_pair_words * 8);
+    if (e == cudaSuccess) e = cudaMemset(r->fc, 0, sizeof(FrameCounters));
+    if (e == cudaSuccess) e = cudaMemset(r->fc_sort, 0, sizeof(FrameCounters));
+    if (e == cudaSuccess) e = cudaMemset(r->epoch, 0, 4);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->host_fc), sizeof(FrameCounters));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        r->release();
+        delete r;
+        return fail(e == cudaErrorMemoryAllocation ? SPL_ERR_OOM : SPL_ERR_CUDA, "renderer setup: %s",
+                    cudaGetErrorString(e));
+    }
+    *out = r;
+    return SPL_OK;
+}
+
+void spl_renderer_destroy(spl_renderer* r) {
+    if (!r) return;
+    cudaDeviceSynchronize();
+    r->release();
+    delete r;
+}
+
+int spl_renderer_reserve(spl_renderer* r, uint32_t width, uint32_t height) {
+    if (!r || width == 0 || height == 0 || width > 65535 || height > 65535)
+        return fail(SPL_ERR_INVALID, "bad reserve arguments");
+    const uint64_t tiles = ceil_div(width, TILE_PIXELS) * ceil_div(height, TILE_PIXELS);
+    return ensure_ranges(r, tiles);
+}
+
+int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
+                     uint32_t height, void* out_device, void* stream) {
+    if (!r || !scene || !camera_to_world || !out_device) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (width == 0 || height == 0 || width > 65535 || height > 65535)
+        return fail(SPL_ERR_INVALID, "viewport %ux%u outside [1, 65535]", width, height);
+    if (scene->n > r->max_n) return fail(SPL_ERR_INVALID, "scene larger than the renderer's max_splat_count");
+    cudaStream_t st = (cudaStream_t)stream;
+    const spl_config& cfg = r->cfg;
+    const uint64_t tiles_x = ceil_div(width, TILE_PIXELS), tiles_y = ceil_div(height, TILE_PIXELS);
+    const uint64_t tiles = tiles_x * tiles_y;
+    if (tiles > r->ranges_cap) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+            return fail(SPL_ERR_INVALID, "call spl_renderer_reserve(%u, %u) before capturing a frame", width, height);
+        int rc = ensure_ranges(r, tiles);
+        if (rc) return rc;
+    }
+    Uniforms u;
+    compute_uniforms(cfg, camera_to_world, width, height, u);
+    const SceneView sv = scene->view();
+    const uint32_t N = (uint32_t)scene->n;
+    const int mode = cfg.depth_sorting;
+    const uint32_t sl = r->spin_limit;
+
+    r->mark(0, st);
+    launch_frame_begin(r->fc, r->epoch, st);
+    launch_cull_key(mode, sv, u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
+    r->mark(1, st);
+    // vertex stage on the side stream, overlapping the depth sort
+    CU(cudaEventRecord(r->ev_fork, st));
+    CU(cudaStreamWaitEvent(r->aux, r->ev_fork, 0));
+    r->mark(9, r->aux);
+    launch_preprocess((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
+                      cfg.use_unaligned_rectangles != 0, sv, u, r->idx, r->fc, r->rec, N, r->aux);
+    r->mark(10, r->aux);
+    CU(cudaEventRecord(r->ev_join, r->aux));
+    const uint32_t* order = nullptr;
+    if (mode != DS_NONE && N > 0) {
+        // four stable 8-bit passes: a -> b -> a -> b -> a; pass 0 takes the compaction slot as value
+        uint32_t* src_k = r->keys_a;
+        const uint32_t* src_v = nullptr;
+        uint32_t* dst_k = r->keys_b;
+        uint32_t* dst_v = r->vals_b;
+        const uint64_t stride = r->sort_tiles() * 256;
+        for (int p = 0; p < 4; ++p) {
+            launch_onesweep(src_k, src_v, dst_k, dst_v, &r->fc->visible, N, r->fc->hist_depth[p],
+                            r->st_sort + p * stride, &r->fc->tile_counter[1 + p], r->epoch, 8 * p, sl, &r->fc->err,
+                            st);
+            uint32_t* next_k = dst_k == r->keys_b ? r->keys_a : r->keys_b;
+            uint32_t* next_v = dst_v == r->vals_b ? r->vals_a : r->vals_b;
+            src_k = dst_k;
+            src_v = dst_v;
+            dst_k = next_k;
+            dst_v = next_v;
+        }
+        order = src_v;  // == vals_a, keys in keys_a
+    }
+    r->mark(2, st);
+    CU(cudaStreamWaitEvent(st, r->ev_join, 0));
+    CU(cudaMemsetAsync(r->ranges, 0, tiles * sizeof(uint2), st));
+    r->mark(3, st);
+    launch_bin(mode, order, r->rec, r->fc, r->epoch, r->st_bin, r->pk_a, r->pv_a, (uint32_t)r->pair_cap,
+               (int)tiles_x, N, sl, st);
+    r->mark(4, st);
+    // stable sort of the pairs by tile id keeps each tile's list in depth order
+    const int passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
+    uint32_t *pk = r->pk_a, *pv = r->pv_a, *qk = r->pk_b, *qv = r->pv_b;
+    const uint64_t pstride = r->pair_tiles() * 256;
+    for (int p = 0; p < passes; ++p) {
+        launch_onesweep(pk, pv, qk, qv, &r->fc->pairs, (uint32_t)r->pair_cap, r->fc->hist_pairs[p],
+                        r->st_pairs + p * pstride, &r->fc->tile_counter[5 + p], r->epoch, 8 * p, sl, &r->fc->err, st);
+        std::swap(pk, qk);
+        std::swap(pv, qv);
+    }
+    r->mark(5, st);
+    launch_tile_ranges(pk, r->fc, (uint32_t)r->pair_cap, r->ranges, st);
+    r->mark(6, st);
+    launch_raster(cfg.use_unaligned_rectangles != 0, cfg.blend_mode, r->ranges, pv, r->rec, u, out_device, st);
+    r->mark(7, st);
+    CU(cudaGetLastError());
+    r->last_stream = st;
+    r->has_frame = true;
+    r->last_w = width;
+    r->last_h = height;
+    r->last_n = N;
+    r->final_pair_vals = pv;
+    return SPL_OK;
+}
+
+int spl_renderer_set_profiling(spl_renderer* r, int enable) {
+    if (!r) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (enable) {
+        for (auto& e : r->ev_prof)
+            if (!e) CU(cudaEventCreate(&e));
+    }
+    r->profiling = enable != 0;
+    return SPL_OK;
+}
+
+int spl_renderer_stage_times(spl_renderer* r, float* ms, int count) {
+    if (!r || !ms || count < SPL_STAGE_COUNT) return fail(SPL_ERR_INVALID, "need %d outputs", SPL_STAGE_COUNT);
+    if (!r->profiling || !r->has_frame) return fail(SPL_ERR_INVALID, "profiling is off or no frame rendered");
+    CU(cudaEventSynchronize(r->ev_prof[7]));
+    CU(cudaEventSynchronize(r->ev_prof[10]));
+    auto el = [&](int a, int b, float* out) -> cudaError_t { return cudaEventElapsedTime(out, r->ev_prof[a], r->ev_prof[b]); };
+    CU(el(0, 1, &ms[SPL_STAGE_CULL]));
+    CU(el(9, 10, &ms[SPL_STAGE_PREPROCESS]));
+    CU(el(1, 2, &ms[SPL_STAGE_DEPTH_SORT]));
+    CU(el(3, 4, &ms[SPL_STAGE_BIN]));
+    CU(el(4, 5, &ms[SPL_STAGE_PAIR_SORT]));
+    CU(el(5, 6, &ms[SPL_STAGE_RANGES]));
+    CU(el(6, 7, &ms[SPL_STAGE_RASTER]));
+    CU(el(0, 7, &ms[SPL_STAGE_FRAME]));
+    return SPL_OK;
+}
+
+int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint32_t height) {
+    if (!r) return 0;
+    const uint64_t tiles = ceil_div(width, TILE_PIXELS) * ceil_div(height, TILE_PIXELS);
+    const int pair_passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
+    const int depth_passes = r->cfg.depth_sorting == DS_NONE ? 0 : 4;
+    // frame_begin, cull, preprocess, depth passes, ranges memset, bin, pair passes, ranges, raster
+    return 1 + 1 + 1 + depth_passes + 1 + 1 + pair_passes + 1 + 1;
+}
+
+int spl_renderer_frame_info(spl_renderer* r, spl_frame_info* info) {
+    if (!r || !info) return fail(SPL_ERR_INVALID, "NULL argument");
+    std::memset(info, 0, sizeof(*info));
+    if (!r->has_frame) return fail(SPL_ERR_INVALID, "no frame rendered yet");
+    CU(cudaMemcpyAsync(r->host_fc, r->fc, sizeof(FrameCounters), cudaMemcpyDeviceToHost, r->last_stream));
+    CU(cudaStreamSynchronize(r->last_stream));
+    const FrameCounters& f = *r->host_fc;
+    info->splat_count = r->last_n;
+    info->visible_count = f.visible;
+    info->draw_count = f.draw;
+    info->pair_count = f.pairs;
+    info->device_error = f.err;
+    info->width = r->last_w;
+    info->height = r->last_h;
+    if (f.err & SPL_DEV_ERR_LOOKBACK) return fail(SPL_ERR_LOOKBACK_TIMEOUT, "a decoupled look-back wait timed out");
+    if (f.err & SPL_DEV_ERR_PAIR_OVERFLOW)
+        return fail(SPL_ERR_CAPACITY, "tile binning needs %u pairs, capacity %llu", f.pairs,
+                    (unsigned long long)r->pair_cap);
+    return SPL_OK;
+}
+
+int spl_renderer_copy_entries(spl_renderer* r, uint32_t* keys_device, uint32_t* indices_device, uint64_t capacity,
+                              void* stream) {
+    if (!r || !keys_device || !indices_device) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (!r->has_frame) return fail(SPL_ERR_INVALID, "no frame rendered yet");
+    if (capacity > r->max_n) capacity = r->max_n;
+    const bool sorted = r->cfg.depth_sorting != DS_NONE;
+    launch_gather_entries(r->keys_a, sorted ? r->vals_a : nullptr, r->idx, r->fc, r->cfg.depth_sorting, keys_device,
+                          indices_device, (uint32_t)capacity, (cudaStream_t)stream);
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
+int spl_renderer_copy_records(spl_renderer* r, float* records_device, uint64_t capacity, void* stream) {
+    if (!r || !records_device) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (capacity > r->max_n) capacity = r->max_n;
+    if (capacity == 0) return SPL_OK;
+    CU(cudaMemcpyAsync(records_device, r->rec, capacity * 64, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return SPL_OK;
+}
+
+int spl_sort_pairs(spl_renderer* r, const uint32_t* keys_in, const uint32_t* values_in, uint32_t* keys_out,
+                   uint32_t* values_out, uint64_t count, uint32_t key_bits, void* stream) {
+    if (!r || !keys_in || !values_in || !keys_out || !values_out) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (count > r->max_n) return fail(SPL_ERR_INVALID, "count %llu above max_splat_count", (unsigned long long)count);
+    if (key_bits == 0 || key_bits > 32 || key_bits % 8 != 0) return fail(SPL_ERR_INVALID, "key_bits %u", key_bits);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (count == 0) return SPL_OK;
+    const int passes = (int)(key_bits / 8);
+    launch_frame_begin(r->fc_sort, r->epoch, st);
+    launch_set_count(&r->fc_sort->visible, (uint32_t)count, st);
+    launch_histogram(keys_in, &r->fc_sort->visible, (uint32_t)count, r->fc_sort->hist_depth[0], st);
+    const uint64_t stride = r->sort_tiles() * 256;
+    const uint32_t* kin = keys_in;
+    const uint32_t* vin = values_in;
+    for (int p = 0; p < passes; ++p) {
+        const bool to_out = ((passes - 1 - p) % 2) == 0;
+        uint32_t* kout = to_out ? keys_out : r->keys_b;
+        uint32_t* vout = to_out ? values_out : r->vals_b;
+        launch_onesweep(kin, vin, kout, vout, &r->fc_sort->visible, (uint32_t)count, r->fc_sort->hist_depth[p],
+                        r->st_sort + p * stride, &r->fc_sort->tile_counter[1 + p], r->epoch, 8 * p, r->spin_limit,
+                        &r->fc_sort->err, st);
+        kin = kout;
+        vin = vout;
+    }
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
+int spl_debug_lookback_timeout(uint32_t spin_limit, int* timed_out) {
+    if (!timed_out) return fail(SPL_ERR_INVALID, "NULL argument");
+    *timed_out = 0;
+    uint64_t* status = nullptr;
+    uint32_t* words = nullptr;
+    int rc = dalloc(&status, 64);
+    if (rc) return rc;
+    rc = dalloc(&words, 4);
+    if (rc) {
+        dfree(status);
+        return rc;
+    }
+    uint32_t host[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemset(status, 0, 64 * 8);
+    if (e == cudaSuccess) e = cudaMemset(words, 0, 16);
+    if (e == cudaSuccess) {
+        launch_lookback_probe(status, words, spin_limit, words + 2, nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(host, words, 16, cudaMemcpyDeviceToHost);
+    dfree(status);
+    dfree(words);
+    if (e != cudaSuccess) return fail(SPL_ERR_CUDA, "look-back probe: %s", cudaGetErrorString(e));
+    *timed_out = (host[3] & SPL_DEV_ERR_LOOKBACK) ? 1 : 0;
+    return SPL_OK;
+}
+
+// ---- scenes ----------------------------------------------------------------------------------------
+
+int spl_scene_create(spl_renderer* r, uint64_t splat_count, spl_scene** out, uint64_t* clamped_count) {
+    if (!r || !out) return fail(SPL_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    spl_scene* s = new (std::nothrow) spl_scene();
+    if (!s) return fail(SPL_ERR_OOM, "host allocation failed");
+    s->renderer = r;
+    cudaGetDevice(&s->device);
+    s->n = splat_count < r->max_n ? splat_count : r->max_n;  // scene.rs:46
+    const uint64_t n = s->n;
+    int rc = SPL_OK;
+    if (!rc) rc = dalloc(&s->x, n);
+    if (!rc) rc = dalloc(&s->y, n);
+    if (!rc) rc = dalloc(&s->z, n);
+    if (!rc) rc = dalloc(&s->rot, n);
+    if (!rc) rc = dalloc(&s->scale_alpha, n);
+    if (!rc) rc = dalloc(&s->sh, n * 48);
+    if (rc) {
+        s->release();
+        delete s;
+        return rc;
+    }
+    // zeroed like a fresh wgpu buffer
+    cudaError_t e = cudaSuccess;
+    if (n) {
+        e = cudaMemset(s->x, 0, n * 4);
+        if (e == cudaSuccess) e = cudaMemset(s->y, 0, n * 4);
+        if (e == cudaSuccess) e = cudaMemset(s->z, 0, n * 4);
+        if (e == cudaSuccess) e = cudaMemset(s->rot, 0, n * 16);
+        if (e == cudaSuccess) e = cudaMemset(s->scale_alpha, 0, n * 16);
+        if (e == cudaSuccess) e = cudaMemset(s->sh, 0, n * 192);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    if (e != cudaSuccess) {
+        s->release();
+        delete s;
+        return fail(SPL_ERR_CUDA, "scene setup: %s", cudaGetErrorString(e));
+    }
+    *out = s;
+    if (clamped_count) *clamped_count = n;
+    return SPL_OK;
+}
+
+void spl_scene_destroy(spl_scene* s) {
+    if (!s) return;
+    cudaDeviceSynchronize();
+    s->release();
+    delete s;
+}
+
+uint64_t spl_scene_splat_count(const spl_scene* s) { return s ? s->n : 0; }
+uint64_t spl_scene_device_bytes(const spl_scene* s) { return s ? s->n * 236ull : 0; }
+
+int spl_scene_load_chunk(spl_scene* s, const void* records, uint64_t start, uint64_t count, void* stream) {
+    if (!s || (!records && count)) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (start >= s->n) return SPL_OK;
+    if (count > s->n - start) count = s->n - start;  // scene.rs:217
+    const float* src = static_cast<const float*>(records);
+    return staged_upload(
+        s, start, count, 62, (cudaStream_t)stream,
+        [&](float* dst, uint64_t first, uint64_t cnt) {
+            std::memcpy(dst, src + (first - start) * 62, cnt * 248);
+            return SPL_OK;
+        },
+        [&](float* dev, uint64_t first, uint64_t cnt, cudaStream_t st) {
+            launch_load_records(dev, (uint32_t)cnt, s->x + first, s->y + first, s->z + first, s->rot + first,
+                                s->scale_alpha + first, s->sh + first * 48, st);
+        });
+}
+
+int spl_scene_load_chunk_file(spl_scene* s, const char* path, uint32_t header_bytes, uint64_t start, uint64_t count,
+                              void* stream) {
+    if (!s || !path) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (start >= s->n) return SPL_OK;
+    if (count > s->n - start) count = s->n - start;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(SPL_ERR_IO, "cannot open %s", path);
+    if (std::fseek(f, (long)(header_bytes + start * 248ull), SEEK_SET) != 0) {
+        std::fclose(f);
+        return fail(SPL_ERR_IO, "seek failed in %s", path);
+    }
+    int rc = staged_upload(
+        s, start, count, 62, (cudaStream_t)stream,
+        [&](float* dst, uint64_t, uint64_t cnt) {
+            if (std::fread(dst, 248, cnt, f) != cnt) return fail(SPL_ERR_IO, "short read in %s", path);
+            return SPL_OK;
+        },
+        [&](float* dev, uint64_t first, uint64_t cnt, cudaStream_t st) {
+            launch_load_records(dev, (uint32_t)cnt, s->x + first, s->y + first, s->z + first, s->rot + first,
+                                s->scale_alpha + first, s->sh + first * 48, st);
+        });
+    std::fclose(f);
+    return rc;
+}
+
+int spl_scene_write_splats(spl_scene* s, const float* splats60, uint64_t start, uint64_t count, void* stream) {
+    if (!s || (!splats60 && count)) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (start >= s->n) return SPL_OK;
+    if (count > s->n - start) count = s->n - start;
+    return staged_upload(
+        s, start, count, 60, (cudaStream_t)stream,
+        [&](float* dst, uint64_t first, uint64_t cnt) {
+            std::memcpy(dst, splats60 + (first - start) * 60, cnt * 240);
+            return SPL_OK;
+        },
+        [&](float* dev, uint64_t first, uint64_t cnt, cudaStream_t st) {
+            launch_splats60_to_soa(dev, (uint32_t)cnt, s->x + first, s->y + first, s->z + first, s->rot + first,
+                                   s->scale_alpha + first, s->sh + first * 48, st);
+        });
+}
+
+int spl_scene_read_splats(const spl_scene* cs, float* splats60, uint64_t start, uint64_t count) {
+    spl_scene* s = const_cast<spl_scene*>(cs);
+    if (!s || (!splats60 && count)) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (start > s->n || count > s->n - start) return fail(SPL_ERR_INVALID, "range outside the scene");
+    std::lock_guard<std::mutex> lk(s->stg_mu);
+    int rc = ensure_staging(s);
+    if (rc) return rc;
+    CU(cudaDeviceSynchronize());
+    uint64_t done = 0;
+    while (done < count) {
+        const uint64_t cnt = (count - done) < CHUNK_RECORDS ? (count - done) : CHUNK_RECORDS;
+        launch_soa_to_splats60(s->view(), (uint32_t)(start + done), (uint32_t)cnt, s->stg.dev[0], nullptr);
+        CU(cudaGetLastError());
+        CU(cudaMemcpy(splats60 + done * 60, s->stg.dev[0], cnt * 240, cudaMemcpyDeviceToHost));
+        done += cnt;
+    }
+    return SPL_OK;
+}
+
+int spl_scene_create_dev_test(spl_renderer* r, spl_scene** out) {
+    int rc = spl_scene_create(r, 3, out, nullptr);
+    if (rc) return rc;
+    float d[3][60];
+    std::memset(d, 0, sizeof(d));
+    for (int i = 0; i < 3; ++i) {  // scene.rs:162-177
+        d[i][0] = 1.0f;
+        d[i][4] = i == 0 ? 1.0f : 0.0f;
+        d[i][5] = i == 1 ? 1.0f : 0.0f;
+        d[i][6] = i == 2 ? 1.0f : 0.0f;
+        d[i][8] = 0.2f;
+        d[i][9] = 0.1f;
+        d[i][10] = 0.05f;
+        d[i][11] = 1.0f;
+        d[i][12] = i == 0 ? 1.0f : 0.0f;
+        d[i][13] = i == 1 ? 1.0f : 0.0f;
+        d[i][14] = i == 2 ? 1.0f : 0.0f;
+    }
+    const uint64_t n = (*out)->n < 3 ? (*out)->n : 3;
+    rc = spl_scene_write_splats(*out, &d[0][0], 0, n, nullptr);
+    if (rc == SPL_OK) {
+        cudaError_t e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) rc = fail(SPL_ERR_CUDA, "dev test upload: %s", cudaGetErrorString(e));
+    }
+    if (rc) {
+        spl_scene_destroy(*out);
+        *out = nullptr;
+    }
+    return rc;
+}
+
+int spl_parse_file_header(const char* path, uint32_t* header_bytes, uint64_t* splat_count) {
+    if (!path || !header_bytes || !splat_count) return fail(SPL_ERR_INVALID, "NULL argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(SPL_ERR_IO, "cannot open %s", path);
+    char line[4096];
+    uint64_t count = 0;
+    bool ended = false;
+    uint64_t pos = 0;
+    while (std::fgets(line, sizeof(line), f)) {  // scene.rs:201-210
+        pos += std::strlen(line);
+        if (std::strcmp(line, "end_header\n") == 0) {
+            ended = true;
+            break;
+        }
+        if (std::strncmp(line, "element vertex ", 15) == 0) {
+            char* endp = nullptr;
+            const unsigned long long v = std::strtoull(line + 15, &endp, 10);
+            if (endp == line + 15 || (*endp != '\n' && *endp != '\0')) {
+                std::fclose(f);
+                return fail(SPL_ERR_IO, "malformed element vertex line in %s", path);
+            }
+            count = v;
+        }
+    }
+    std::fclose(f);
+    if (!ended) return fail(SPL_ERR_IO, "no end_header in %s", path);
+    if (pos > 0xFFFFFFFFull) return fail(SPL_ERR_IO, "header too long in %s", path);
+    *header_bytes = (uint32_t)pos;
+    *splat_count = count;
+    return SPL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,595 @@
+// Projection side of the splat pipeline (sm_103a):
+//   k_frame_begin   - per-frame counter reset + epoch bump (replaces buffer clears, renderer.rs:412,422-427)
+//   k_cull_key      - worldToClipSpace + isInFrustum + depth key + digit histograms (radixSortA,
+//                     shaders.wgsl:298-336) fused with ORDERED stream compaction of the visible splats
+//                     (warp ballots + decoupled look-back), so only visible keys are sorted
+//   k_preprocess    - the vertex stage (shaders.wgsl:507-573): SH colour, exact perspective conic of the
+//                     ellipsoid, its decomposition and the rotated rectangle, emitted once per visible
+//                     splat as a 64-byte screen-space record for the compute rasteriser
+//   k_load_records  - Scene::load_chunk transform (scene.rs:225-250) on the device
+//
+// Compiled with -fmad=false: all FP32 expressions follow the WGSL operation order and are
+// bit-identical to the oracle's FP32 restatement.
+#include <cstdio>
+
+#include "spl_device.cuh"
+
+namespace spl {
+
+// ------------------------------------------------------------------------------------------------
+__global__ void k_frame_begin(FrameCounters* fc, uint32_t* epoch_word) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(fc);
+    const uint32_t nwords = sizeof(FrameCounters) / 4;
+    for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) w[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t e = *epoch_word + 1u;
+        if (e == 0u) e = 1u;  // epoch 0 marks never-written status words
+        *epoch_word = e;
+        fc->epoch = e;
+    }
+}
+
+void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st) {
+    k_frame_begin<<<1, 256, 0, st>>>(fc, epoch_word);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Cull + key + histogram + ordered compaction.  One CTA handles 4096 consecutive splats; warp w owns
+// splats [w*512, w*512+512) of the tile and lane l handles elements w*512 + 32*j + l, so loads are
+// coalesced and the ballot order is the index order.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_cull_key(SceneView s, Uniforms u, FrameCounters* fc,
+                                                  const uint32_t* __restrict__ epoch_word, uint64_t* status,
+                                                  uint32_t* __restrict__ keys_out, uint32_t* __restrict__ idx_out,
+                                                  uint32_t spin_limit) {
+    __shared__ uint32_t s_hist[1024];
+    __shared__ uint32_t s_wcnt[8];
+    __shared__ uint32_t s_tile, s_epoch, s_base;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
+    for (uint32_t i = tid; i < 1024u; i += 256u) s_hist[i] = 0u;
+    if (tid == 0) {
+        s_tile = atomicAdd(&fc->tile_counter[0], 1u);
+        s_epoch = *epoch_word;
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile, epoch = s_epoch, n = s.n;
+    const uint32_t ntiles = (n + CULL_TILE - 1) / CULL_TILE;
+    const uint32_t base = tile * CULL_TILE + w * 512u + lane;
+
+    float px[16], py[16], pz[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const uint32_t e = base + 32u * j;
+        if (e < n) {
+            px[j] = __ldg(s.x + e);
+            py[j] = __ldg(s.y + e);
+            pz[j] = __ldg(s.z + e);
+        } else {
+            px[j] = py[j] = pz[j] = 0.0f;
+        }
+    }
+    uint32_t key[16], pos[16];
+    uint32_t vis_bits = 0u, wtotal = 0u, all_ones = 0u;
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const uint32_t e = base + 32u * j;
+        float h[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            h[r] = ((u.vp[0 * 4 + r] * px[j] + u.vp[1 * 4 + r] * py[j]) + u.vp[2 * 4 + r] * pz[j]) + u.vp[3 * 4 + r] * 1.0f;
+        bool vis;
+        uint32_t k;
+        if (MODE == DS_CPU) {
+            // renderer.rs:381-387: reciprocal multiply, no epsilon, key = bits(z)
+            const float rw = 1.0f / h[3];
+            const float cx = h[0] * rw, cy = h[1] * rw, cz = h[2] * rw;
+            vis = fabsf(cx) < u.tol && fabsf(cy) < u.tol && fabsf(cz - 0.5f) < 0.5f;
+            k = __float_as_uint(cz);
+        } else {
+            // shaders.wgsl:54-61, 318-324
+            const float den = h[3] + 1e-7f;
+            const float cx = h[0] / den, cy = h[1] / den, cz = h[2] / den;
+            vis = fabsf(cx) < u.tol && fabsf(cy) < u.tol && fabsf(cz - 0.5f) < 0.5f;
+            k = sat_u32(cz * 65535.0f) << 16;
+            k |= sat_u32((cx * 0.5f + 0.5f) * 255.0f) << 8;
+            k |= sat_u32((cy * 0.5f + 0.5f) * 255.0f);
+        }
+        vis = vis && e < n;
+        const uint32_t b = __ballot_sync(FULL_MASK, vis);
+        pos[j] = wtotal + __popc(b & lt);
+        wtotal += __popc(b);
+        key[j] = k;
+        if (vis) {
+            vis_bits |= 1u << j;
+            atomicAdd(&s_hist[k & 255u], 1u);
+            atomicAdd(&s_hist[256u + ((k >> 8) & 255u)], 1u);
+            atomicAdd(&s_hist[512u + ((k >> 16) & 255u)], 1u);
+            atomicAdd(&s_hist[768u + (k >> 24)], 1u);
+            all_ones += k == 0xFFFFFFFFu;
+        }
+    }
+    if (lane == 0) s_wcnt[w] = wtotal;
+    __syncthreads();
+    uint32_t wpre = 0, ttot = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 8; ++i) {
+        const uint32_t c = s_wcnt[i];
+        wpre += i < w ? c : 0u;
+        ttot += c;
+    }
+    if (w == 0) {
+        if (lane == 0) lb_store(status + tile, lb_pack(epoch, tile == 0 ? LB_INC : LB_AGG, ttot));
+        const uint32_t excl = tile == 0 ? 0u : lookback_single(status, tile, epoch, spin_limit, &fc->err);
+        if (lane == 0) {
+            if (tile != 0) lb_store(status + tile, lb_pack(epoch, LB_INC, excl + ttot));
+            s_base = excl;
+            if (tile == ntiles - 1) fc->visible = excl + ttot;
+        }
+    }
+    __syncthreads();
+    const uint32_t out0 = s_base + wpre;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        if (vis_bits & (1u << j)) {
+            keys_out[out0 + pos[j]] = key[j];
+            idx_out[out0 + pos[j]] = base + 32u * j;
+        }
+    }
+    for (uint32_t i = tid; i < 1024u; i += 256u) {
+        const uint32_t v = s_hist[i];
+        if (v) atomicAdd(&fc->hist_depth[0][0] + i, v);
+    }
+    if (MODE != DS_CPU) {
+        const uint32_t a = __reduce_add_sync(FULL_MASK, all_ones);
+        if (lane == 0 && a) atomicAdd(&fc->keys_all_ones, a);
+    }
+}
+
+void launch_cull_key(int mode, const SceneView& s, const Uniforms& u, FrameCounters* fc, const uint32_t* epoch_word,
+                     uint64_t* status, uint32_t* keys_out, uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st) {
+    if (s.n == 0) return;
+    const uint32_t grid = (s.n + CULL_TILE - 1) / CULL_TILE;
+    if (mode == DS_CPU)
+        k_cull_key<DS_CPU><<<grid, 256, 0, st>>>(s, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
+    else
+        k_cull_key<DS_GPU><<<grid, 256, 0, st>>>(s, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Vertex-stage math (shaders.wgsl), FP32, in the WGSL operation order.
+struct M3 {
+    float m[9];  // column-major m[c*3 + r]
+};
+
+__device__ __forceinline__ M3 mul3(const M3& A, const M3& B) {
+    M3 t;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            t.m[j * 3 + i] = (A.m[0 * 3 + i] * B.m[j * 3 + 0] + A.m[1 * 3 + i] * B.m[j * 3 + 1]) + A.m[2 * 3 + i] * B.m[j * 3 + 2];
+    return t;
+}
+__device__ __forceinline__ M3 transpose3(const M3& A) {
+    M3 t;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) t.m[c * 3 + r] = A.m[r * 3 + c];
+    return t;
+}
+
+// quatToMat (shaders.wgsl:63-79)
+__device__ __forceinline__ M3 quat_to_mat(float4 p) {
+    const float s2 = 1.41421356237309504880f;
+    const float qx = p.x * s2, qy = p.y * s2, qz = p.z * s2, qw = p.w * s2;
+    const float yy = qy * qy, yz = qy * qz, yw = qy * qw, yx = qy * qx;
+    const float zz = qz * qz, zw = qz * qw, zx = qz * qx;
+    const float ww = qw * qw, wx = qw * qx;
+    M3 m;
+    m.m[0] = (1.0f - zz) - ww; m.m[1] = yz + wx;          m.m[2] = yw - zx;
+    m.m[3] = yz - wx;          m.m[4] = (1.0f - yy) - ww; m.m[5] = zw + yx;
+    m.m[6] = yw + zx;          m.m[7] = zw - yx;          m.m[8] = (1.0f - yy) - zz;
+    return m;
+}
+
+__device__ __forceinline__ M3 camera3(const Uniforms& u) {
+    M3 c;
+#pragma unroll
+    for (int col = 0; col < 3; ++col)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) c.m[col * 3 + r] = u.camera[col * 4 + r];
+    return c;
+}
+
+// projectedContourOfEllipsoid (shaders.wgsl:125-169)
+__device__ __forceinline__ M3 projected_contour(const Uniforms& u, float sx, float sy, float sz, float4 rot, float tx,
+                                                float ty, float tz) {
+    const M3 C = camera3(u);
+    M3 T = quat_to_mat(rot);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        T.m[0 * 3 + r] = T.m[0 * 3 + r] / sx;
+        T.m[1 * 3 + r] = T.m[1 * 3 + r] / sy;
+        T.m[2 * 3 + r] = T.m[2 * 3 + r] / sz;
+    }
+    const float ro0 = u.camera[12] - tx, ro1 = u.camera[13] - ty, ro2 = u.camera[14] - tz;
+    float l[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) l[i] = (ro0 * T.m[i * 3 + 0] + ro1 * T.m[i * 3 + 1]) + ro2 * T.m[i * 3 + 2];
+    const float l0 = l[0] * l[0], l1 = l[1] * l[1], l2 = l[2] * l[2];
+    const float dx = (1.0f - l1) - l2, dy = (1.0f - l0) - l2, dz = (1.0f - l0) - l1;
+    const float trx = l[1] * l[2], try_ = l[0] * l[2], trz = l[0] * l[1];
+    M3 A;
+    A.m[0] = dx;   A.m[1] = trz;  A.m[2] = try_;
+    A.m[3] = trz;  A.m[4] = dy;   A.m[5] = trx;
+    A.m[6] = try_; A.m[7] = trx;  A.m[8] = dz;
+    const M3 T2 = mul3(transpose3(C), T);
+    return mul3(mul3(T2, A), transpose3(T2));
+}
+
+// projectedCovarianceOfEllipsoid (shaders.wgsl:99-118)
+__device__ __forceinline__ M3 projected_covariance(const Uniforms& u, float sx, float sy, float sz, float4 rot,
+                                                   float tx, float ty, float tz) {
+    const M3 C = camera3(u);
+    M3 T = quat_to_mat(rot);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        T.m[0 * 3 + r] = T.m[0 * 3 + r] * sx;
+        T.m[1 * 3 + r] = T.m[1 * 3 + r] * sy;
+        T.m[2 * 3 + r] = T.m[2 * 3 + r] * sz;
+    }
+    float v[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        v[r] = ((u.view[0 * 4 + r] * tx + u.view[1 * 4 + r] * ty) + u.view[2 * 4 + r] * tz) + u.view[3 * 4 + r] * 1.0f;
+    v[0] = fminf(fmaxf(v[0] / v[2], -1.0f), 1.0f) * v[2];
+    v[1] = fminf(fmaxf(v[1] / v[2], -1.0f), 1.0f) * v[2];
+    const float zz = v[2] * v[2];
+    M3 J;
+    J.m[0] = 1.0f / v[2]; J.m[1] = 0.0f;        J.m[2] = (-v[0]) / zz;
+    J.m[3] = 0.0f;        J.m[4] = 1.0f / v[2]; J.m[5] = (-v[1]) / zz;
+    J.m[6] = 0.0f;        J.m[7] = 0.0f;        J.m[8] = 0.0f;
+    const M3 Tm = mul3(mul3(transpose3(T), C), J);
+    return mul3(transpose3(Tm), Tm);
+}
+
+__device__ __forceinline__ float wgsl_sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+
+__constant__ float c_shc[16] = {
+    0.28209479177387814f,  -0.4886025119029199f, 0.4886025119029199f,  -0.4886025119029199f,
+    1.0925484305920792f,   -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
+    0.5462742152960396f,   -0.5900435899266435f, 2.890611442640554f,   -0.4570457994644658f,
+    0.3731763325901154f,   -0.4570457994644658f, 1.445305721320277f,   -0.5900435899266435f,
+};
+
+template <int SHO>
+__device__ __forceinline__ void load_sh(const float* __restrict__ sh, uint32_t i, float* out) {
+    constexpr int NF = 3 * (SHO + 1) * (SHO + 1);
+    constexpr int NV = (NF + 3) / 4;
+    const float4* p = reinterpret_cast<const float4*>(sh + (size_t)i * 48);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const float4 v = __ldg(p + k);
+        out[4 * k + 0] = v.x;
+        if (4 * k + 1 < 48) out[4 * k + 1] = v.y;
+        if (4 * k + 2 < 48) out[4 * k + 2] = v.z;
+        if (4 * k + 3 < 48) out[4 * k + 3] = v.w;
+    }
+}
+
+// sphericalHarmonicsLookup (shaders.wgsl:268-294)
+template <int SHO>
+__device__ __forceinline__ float sh_channel(const float* sh, int c, float x, float y, float z, float xx, float yy,
+                                            float zz) {
+    float col = 0.5f;
+    col = col + c_shc[0] * sh[c];
+    if (SHO > 0) {
+        col = col + (c_shc[1] * sh[3 + c]) * y;
+        col = col + (c_shc[2] * sh[6 + c]) * z;
+        col = col + (c_shc[3] * sh[9 + c]) * x;
+    }
+    if (SHO > 1) {
+        col = col + ((c_shc[4] * sh[12 + c]) * x) * y;
+        col = col + ((c_shc[5] * sh[15 + c]) * y) * z;
+        col = col + (c_shc[6] * sh[18 + c]) * ((2.0f * zz - xx) - yy);
+        col = col + ((c_shc[7] * sh[21 + c]) * x) * z;
+        col = col + (c_shc[8] * sh[24 + c]) * (xx - yy);
+    }
+    if (SHO > 2) {
+        col = col + ((c_shc[9] * sh[27 + c]) * y) * (3.0f * xx - yy);
+        col = col + (((c_shc[10] * sh[30 + c]) * x) * y) * z;
+        col = col + ((c_shc[11] * sh[33 + c]) * y) * ((4.0f * zz - xx) - yy);
+        col = col + ((c_shc[12] * sh[36 + c]) * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
+        col = col + ((c_shc[13] * sh[39 + c]) * x) * ((4.0f * zz - xx) - yy);
+        col = col + ((c_shc[14] * sh[42 + c]) * z) * (xx - yy);
+        col = col + ((c_shc[15] * sh[45 + c]) * x) * (xx - 3.0f * yy);
+    }
+    return col;
+}
+
+template <int SHO, bool COV, bool RECT>
+__global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
+                                                    const FrameCounters* __restrict__ fc, float4* __restrict__ rec) {
+    const uint32_t V = fc->visible;
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < V; slot += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(idx + slot);
+        const float cx = __ldg(s.x + i), cy = __ldg(s.y + i), cz = __ldg(s.z + i);
+        const float4 rot = __ldg(s.rot + i);
+        const float4 sca = __ldg(s.scale_alpha + i);
+        float sh[48];
+        load_sh<SHO>(s.sh, i, sh);
+        // colour (shaders.wgsl:531-532)
+        const float vx = cx - u.camera[12], vy = cy - u.camera[13], vz = cz - u.camera[14];
+        const float len = sqrtf((vx * vx + vy * vy) + vz * vz);
+        const float dx = vx / len, dy = vy / len, dz = vz / len;
+        const float dxx = dx * dx, dyy = dy * dy, dzz = dz * dz;
+        const float cr = sh_channel<SHO>(sh, 0, dx, dy, dz, dxx, dyy, dzz);
+        const float cg = sh_channel<SHO>(sh, 1, dx, dy, dz, dxx, dyy, dzz);
+        const float cb = sh_channel<SHO>(sh, 2, dx, dy, dz, dxx, dyy, dzz);
+        // conic + decomposition (shaders.wgsl:533-542)
+        const float sx = sca.x * u.splat_scale, sy = sca.y * u.splat_scale, sz = sca.z * u.splat_scale;
+        const M3 M = projected_contour(u, sx, sy, sz, rot, cx, cy, cz);
+        const float Mxx = M.m[0], Mxy = M.m[1], Mxz = M.m[2], Myy = M.m[4], Myz = M.m[5], Mzz = M.m[8];
+        // extractTranslationOfEllipse (shaders.wgsl:179-191)
+        const float disc = Mxx * Myy - Mxy * Mxy;
+        const float inv = 1.0f / disc;
+        const float t0 = (Mxy * Myz - Myy * Mxz) * inv;
+        const float t1 = (Mxy * Mxz - Mxx * Myz) * inv;
+        // extractRotationOfEllipse (shaders.wgsl:193-215)
+        const float ra = (Mxx - Myy) * (Mxx - Myy);
+        const float rb = ra + (4.0f * Mxy) * Mxy;
+        const float rc = 0.5f * sqrtf(ra / rb);
+        float rj = sqrtf(0.5f - rc);
+        float rk = ((-sqrtf(0.5f + rc)) * wgsl_sign(Mxy)) * wgsl_sign(Mxx - Myy);
+        if (Mxy < 0.0f || Mxx - Myy < 0.0f) {
+            rk = -rk;
+            rj = -rj;
+        }
+        if (Mxx - Myy < 0.0f) {
+            const float tmp = rj;
+            rj = -rk;
+            rk = tmp;
+        }
+        float ax0, ax1;
+        if (COV) {
+            // extractScaleOfCovariance(projectedCovarianceOfEllipsoid) (shaders.wgsl:240-246, 99-118)
+            const M3 P = projected_covariance(u, sx, sy, sz, rot, cx, cy, cz);
+            const float pxx = P.m[0], pxy = P.m[1], pyy = P.m[4];
+            const float a = (pxx - pyy) * (pxx - pyy);
+            const float b = sqrtf(a + (4.0f * pxy) * pxy);
+            ax0 = sqrtf(((pxx + pyy) + b) * 0.5f);
+            ax1 = sqrtf(((pxx + pyy) - b) * 0.5f);
+        } else {
+            // extractScaleOfEllipse (shaders.wgsl:217-237)
+            const float d = ((2.0f * Mxy) * rj) * rk;
+            const float e = Mzz - (((Mxx * t0) * t0 + (Myy * t1) * t1) + ((2.0f * Mxy) * t0) * t1);
+            ax0 = sqrtf(fabsf(e / (((Mxx * rk) * rk + (Myy * rj) * rj) - d)));
+            ax1 = sqrtf(fabsf(e / (((Mxx * rj) * rj + (Myy * rk) * rk) + d)));
+        }
+        // rect basis (shaders.wgsl:543-547) and its inverse (shaders.wgsl:563-566), folded with the
+        // pixel -> view-plane mapping so that tc is affine in the pixel centre.
+        const float sa = u.bias + ax0, sb = u.bias + ax1;
+        const float Xx = rk * sa, Xy = (-rj) * sa;
+        const float Yx = rj * sb, Yy = rk * sb;
+        const float det = Xx * Yy - Xy * Yx;
+        const float idet = 1.0f / det;
+        const float i00 = Yy * idet, i01 = (-Yx) * idet, i10 = (-Xy) * idet, i11 = Xx * idet;
+        const float vw = u.view_size[0], vh = u.view_size[1];
+        const float Wf = (float)u.image_size[0], Hf = (float)u.image_size[1];
+        const float psx = (2.0f * vw) / Wf, psy = -((2.0f * vh) / Hf);
+        const float bx = (-vw) - t0, by = vh - t1;
+        const float A00 = i00 * psx, A01 = i01 * psy, B0 = i00 * bx + i01 * by;
+        const float A10 = i10 * psx, A11 = i11 * psy, B1 = i10 * bx + i11 * by;
+        const float m = u.margin;
+        float ex, ey, R = 0.0f;
+        if (RECT) {
+            ex = m * (fabsf(Xx) + fabsf(Yx));
+            ey = m * (fabsf(Xy) + fabsf(Yy));
+        } else {
+            R = sqrtf(fmaxf(Xx * Xx + Xy * Xy, Yx * Yx + Yy * Yy)) * m;
+            ex = R;
+            ey = R;
+        }
+        const float cxp = (t0 + vw) / psx, exq = ex / psx;
+        const float cyp = (t1 - vh) / psy, eyq = ey / (-psy);
+        const float fx0 = floorf(cxp - exq) - 1.0f, fx1 = ceilf(cxp + exq) + 1.0f;
+        const float fy0 = floorf(cyp - eyq) - 1.0f, fy1 = ceilf(cyp + eyq) + 1.0f;
+        const float al = sca.w;
+        bool ok = isfinite(A00) && isfinite(A01) && isfinite(B0) && isfinite(A10) && isfinite(A11) && isfinite(B1) &&
+                  isfinite(cr) && isfinite(cg) && isfinite(cb) && isfinite(fx0) && isfinite(fx1) && isfinite(fy0) &&
+                  isfinite(fy1) && isfinite(R) && isfinite(bx) && isfinite(by) && (al >= 1.0f / 255.0f);
+        uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+        if (ok) {
+            const float cx0 = fmaxf(fx0, 0.0f), cx1 = fminf(fx1, Wf - 1.0f);
+            const float cy0 = fmaxf(fy0, 0.0f), cy1 = fminf(fy1, Hf - 1.0f);
+            if (cx0 <= cx1 && cy0 <= cy1) {
+                lo = (uint32_t)(int)cx0 | ((uint32_t)(int)cy0 << 16);
+                hi = (uint32_t)(int)cx1 | ((uint32_t)(int)cy1 << 16);
+            }
+        }
+        float4* o = rec + (size_t)slot * 4;
+        o[0] = make_float4(A00, A01, B0, A10);
+        o[1] = make_float4(A11, B1, al, __uint_as_float(lo));
+        o[2] = make_float4(cr, cg, cb, __uint_as_float(hi));
+        o[3] = RECT ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : make_float4(bx, by, R, 0.0f);
+    }
+}
+
+template <int SHO, bool COV>
+static void launch_pre2(bool rect, dim3 g, const SceneView& s, const Uniforms& u, const uint32_t* idx,
+                        const FrameCounters* fc, float4* rec, cudaStream_t st) {
+    if (rect)
+        k_preprocess<SHO, COV, true><<<g, 256, 0, st>>>(s, u, idx, fc, rec);
+    else
+        k_preprocess<SHO, COV, false><<<g, 256, 0, st>>>(s, u, idx, fc, rec);
+}
+template <int SHO>
+static void launch_pre1(bool cov, bool rect, dim3 g, const SceneView& s, const Uniforms& u, const uint32_t* idx,
+                        const FrameCounters* fc, float4* rec, cudaStream_t st) {
+    if (cov)
+        launch_pre2<SHO, true>(rect, g, s, u, idx, fc, rec, st);
+    else
+        launch_pre2<SHO, false>(rect, g, s, u, idx, fc, rec, st);
+}
+
+void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
+                       const uint32_t* idx, const FrameCounters* fc, float4* rec, uint32_t max_n, cudaStream_t st) {
+    if (max_n == 0) return;
+    uint32_t blocks = (max_n + 255) / 256;
+    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    const dim3 g(blocks);
+    switch (sh_order) {
+        case 0: launch_pre1<0>(covariance, rect, g, s, u, idx, fc, rec, st); break;
+        case 1: launch_pre1<1>(covariance, rect, g, s, u, idx, fc, rec, st); break;
+        case 2: launch_pre1<2>(covariance, rect, g, s, u, idx, fc, rec, st); break;
+        default: launch_pre1<3>(covariance, rect, g, s, u, idx, fc, rec, st); break;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Loader: 62-float PLY records -> SoA (scene.rs:225-250).  A block stages 256 records in shared
+// memory with coalesced 16-byte loads, transforms one record per thread, and writes the 48 SH
+// floats of its 256 splats back as one contiguous, coalesced range.
+constexpr int LOAD_BLOCK = 256;
+
+__global__ void __launch_bounds__(LOAD_BLOCK) k_load_records(const float* __restrict__ recs, uint32_t count,
+                                                             float* x, float* y, float* z, float4* rot,
+                                                             float4* scale_alpha, float* sh) {
+    extern __shared__ float4 s_buf4[];
+    float* s_buf = reinterpret_cast<float*>(s_buf4);
+    const uint32_t first = blockIdx.x * LOAD_BLOCK;
+    const uint32_t nrec = min((uint32_t)LOAD_BLOCK, count - first);
+    const uint32_t nflt = nrec * 62u;
+    const float* src = recs + (size_t)first * 62u;  // 256*62*4 bytes per block: 16-byte aligned
+    const uint32_t nvec = nflt / 4u;
+    for (uint32_t k = threadIdx.x; k < nvec; k += LOAD_BLOCK) s_buf4[k] = __ldg(reinterpret_cast<const float4*>(src) + k);
+    for (uint32_t k = nvec * 4u + threadIdx.x; k < nflt; k += LOAD_BLOCK) s_buf[k] = __ldg(src + k);
+    __syncthreads();
+    const uint32_t t = threadIdx.x;
+    if (t < nrec) {
+        const float* r = s_buf + t * 62u;
+        const uint32_t i = first + t;
+        const float q0 = r[58], q1 = r[59], q2 = r[60], q3 = r[61];
+        const float inv = 1.0f / sqrtf(((q0 * q0 + q1 * q1) + q2 * q2) + q3 * q3);
+        rot[i] = make_float4(q0 * inv, q1 * inv, q2 * inv, q3 * inv);
+        x[i] = r[0];
+        y[i] = r[1];
+        z[i] = r[2];
+        const float avg = ((r[55] + r[56]) + r[57]) / 3.0f;
+        const float lo = avg - 5.0f, hi = avg + 5.0f;
+        const float s0 = spl_expf(fminf(fmaxf(r[55], lo), hi));
+        const float s1 = spl_expf(fminf(fmaxf(r[56], lo), hi));
+        const float s2 = spl_expf(fminf(fmaxf(r[57], lo), hi));
+        const float a = 1.0f / (1.0f + spl_expf(-r[54]));
+        scale_alpha[i] = make_float4(s0, s1, s2, a);
+    }
+    float* dst = sh + (size_t)first * 48u;
+    for (uint32_t k = threadIdx.x; k < nrec * 48u; k += LOAD_BLOCK) {
+        const uint32_t rr = k / 48u, c = k - rr * 48u;
+        dst[k] = s_buf[rr * 62u + 6u + c];
+    }
+}
+
+void launch_load_records(const float* records62, uint32_t count, float* x, float* y, float* z, float4* rot,
+                         float4* scale_alpha, float* sh, cudaStream_t st) {
+    if (count == 0) return;
+    static bool attr = false;
+    const int smem = LOAD_BLOCK * 62 * 4;
+    if (!attr) {
+        cudaFuncSetAttribute(k_load_records, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+    }
+    const uint32_t grid = (count + LOAD_BLOCK - 1) / LOAD_BLOCK;
+    k_load_records<<<grid, LOAD_BLOCK, smem, st>>>(records62, count, x, y, z, rot, scale_alpha, sh);
+}
+
+// 60-float device splats of the reference (scene.rs:32, shaders.wgsl:28-35) <-> SoA.
+__global__ void k_splats60_to_soa(const float* __restrict__ s60, uint32_t count, float* x, float* y, float* z,
+                                  float4* rot, float4* scale_alpha, float* sh) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float4* r = reinterpret_cast<const float4*>(s60 + (size_t)i * 60);
+        const float4 a = r[0], b = r[1], c = r[2];
+        rot[i] = a;
+        x[i] = b.x;
+        y[i] = b.y;
+        z[i] = b.z;
+        scale_alpha[i] = c;
+        float4* d = reinterpret_cast<float4*>(sh + (size_t)i * 48);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) d[k] = r[3 + k];
+    }
+}
+
+__global__ void k_soa_to_splats60(SceneView s, uint32_t start, uint32_t count, float* s60) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const uint32_t i = start + t;
+        float4* r = reinterpret_cast<float4*>(s60 + (size_t)t * 60);
+        r[0] = s.rot[i];
+        r[1] = make_float4(s.x[i], s.y[i], s.z[i], 0.0f);
+        r[2] = s.scale_alpha[i];
+        const float4* q = reinterpret_cast<const float4*>(s.sh + (size_t)i * 48);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) r[3 + k] = q[k];
+    }
+}
+
+void launch_splats60_to_soa(const float* s60, uint32_t count, float* x, float* y, float* z, float4* rot,
+                            float4* scale_alpha, float* sh, cudaStream_t st) {
+    if (count == 0) return;
+    uint32_t grid = (count + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    k_splats60_to_soa<<<grid, 256, 0, st>>>(s60, count, x, y, z, rot, scale_alpha, sh);
+}
+
+void launch_soa_to_splats60(const SceneView& s, uint32_t start, uint32_t count, float* s60, cudaStream_t st) {
+    if (count == 0) return;
+    uint32_t grid = (count + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    k_soa_to_splats60<<<grid, 256, 0, st>>>(s, start, count, s60);
+}
+
+// Sorted entries (key, splat index) for readback (the reference's commented debug readback,
+// renderer.rs:456-464).  slots == nullptr for the unsorted (None) mode.
+__global__ void k_gather_entries(const uint32_t* keys, const uint32_t* slots, const uint32_t* idx,
+                                 const FrameCounters* fc, uint32_t* keys_out, uint32_t* idx_out, uint32_t cap) {
+    const uint32_t V = min(fc->visible, cap);
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < V; r += gridDim.x * blockDim.x) {
+        if (slots) {
+            keys_out[r] = keys[r];
+            idx_out[r] = idx[slots[r]];
+        } else {
+            keys_out[r] = keys[r];
+            idx_out[r] = idx[r];
+        }
+    }
+}
+
+void launch_gather_entries(const uint32_t* keys, const uint32_t* slots, const uint32_t* idx, const FrameCounters* fc,
+                           int mode, uint32_t* keys_out, uint32_t* idx_out, uint32_t cap, cudaStream_t st) {
+    (void)mode;
+    if (cap == 0) return;
+    uint32_t grid = (cap + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    k_gather_entries<<<grid, 256, 0, st>>>(keys, slots, idx, fc, keys_out, idx_out, cap);
+}
+
+// Fault-free check of the bounded look-back: one warp acts as tile 1 of a scan whose tile 0 never
+// publishes (status[0] is never written).  The wait runs out after spin_limit polls, raises the
+// error bit and returns; out[0] = prefix it gave up with, out[1] = error word.
+__global__ void k_lookback_probe(uint64_t* status, uint32_t* err, uint32_t spin_limit, uint32_t* out) {
+    const uint32_t excl = lookback_single(status, 1u, 7u, spin_limit, err);
+    __syncwarp();
+    if (threadIdx.x == 0) {
+        out[0] = excl;
+        out[1] = ld_relaxed_u32(err);
+    }
+}
+
+void launch_lookback_probe(uint64_t* status, uint32_t* err, uint32_t spin_limit, uint32_t* out, cudaStream_t st) {
+    k_lookback_probe<<<1, 32, 0, st>>>(status, err, spin_limit, out);
+}
+
+}  // namespace spl

@@ -1,0 +1,269 @@
+// Compute rasteriser for the splat records (sm_103a).  The reference draws each splat as a rotated
+// rectangle (triangle strip, renderer.rs:275-283) through the fixed-function rasteriser, runs the
+// Gaussian fragment (shaders.wgsl:580-592) and blends front-to-back into a Bgra8Unorm target with
+// destination alpha as transmittance (renderer.rs:260-271).  There is no fixed-function unit here,
+// so the frame is tiled into 16x16-pixel tiles:
+//   k_bin          - for each drawn entry in depth order, the tiles its pixel box touches; emitted as
+//                    (tile id, record slot) pairs at offsets from a decoupled look-back scan, with
+//                    load-balanced emission inside the CTA and the tile-id digit histograms
+//   (2 onesweep passes over the 16-bit tile ids: stable, so each tile's list stays in depth order)
+//   k_tile_ranges  - start/end of each tile's run in the sorted pair list
+//   k_raster       - one CTA per tile, one thread per pixel; records staged through shared memory in
+//                    batches of 256, warp-uniform box rejection, exact coverage test, falloff, blend,
+//                    and early exit once every pixel of the tile is opaque
+#include "spl_device.cuh"
+
+namespace spl {
+
+// ------------------------------------------------------------------------------------------------
+template <bool ORDERED>
+__global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order, const float4* __restrict__ rec,
+                                             FrameCounters* fc, int mode, const uint32_t* __restrict__ epoch_word,
+                                             uint64_t* status, uint32_t* __restrict__ pair_keys,
+                                             uint32_t* __restrict__ pair_vals, uint32_t pair_cap, int tiles_x,
+                                             uint32_t spin_limit) {
+    __shared__ uint32_t s_off[BIN_TILE];  // exclusive pair offsets of the tile's entries
+    __shared__ uint32_t s_slot[BIN_TILE];
+    __shared__ uint32_t s_box[BIN_TILE];  // tx0 | ty0 << 16
+    __shared__ uint16_t s_bw[BIN_TILE];
+    __shared__ uint32_t s_hist[768];
+    __shared__ uint32_t s_scan[8];
+    __shared__ uint32_t s_tile, s_epoch, s_base, s_draw;
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        s_tile = atomicAdd(&fc->tile_counter[8], 1u);
+        s_epoch = *epoch_word;
+        const uint32_t V = fc->visible;
+        uint32_t draw = V;
+        if (mode == DS_GPU) draw = V - fc->keys_all_ones;
+        else if (mode == DS_GPU_INDIRECT) draw = V - fc->hist_depth[3][255];
+        s_draw = draw;
+    }
+    s_hist[tid] = 0u;
+    s_hist[tid + 256] = 0u;
+    s_hist[tid + 512] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile, epoch = s_epoch, draw = s_draw;
+    const uint32_t ntiles = (draw + BIN_TILE - 1) / BIN_TILE;
+    if (tile >= ntiles) {
+        if (tile == 0 && tid == 0) {  // nothing to draw at all
+            fc->draw = 0;
+            fc->pairs = 0;
+        }
+        return;
+    }
+    if (tile == 0 && tid == 0) fc->draw = draw;
+    // per-entry tile counts (4 consecutive entries per thread keep the thread order = depth order)
+    uint32_t cnt[4], tsum = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const uint32_t r = tile * BIN_TILE + tid * 4u + e;
+        uint32_t c = 0, slot = 0, box = 0, bw = 0;
+        if (r < draw) {
+            slot = ORDERED ? __ldg(order + r) : r;
+            const float4 q1 = __ldg(rec + (size_t)slot * 4 + 1);
+            const float4 q2 = __ldg(rec + (size_t)slot * 4 + 2);
+            const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
+            const uint32_t x0 = lo & 0xFFFFu, y0 = lo >> 16, x1 = hi & 0xFFFFu, y1 = hi >> 16;
+            if (x0 <= x1 && y0 <= y1) {
+                const uint32_t tx0 = x0 / TILE_PIXELS, tx1 = x1 / TILE_PIXELS;
+                const uint32_t ty0 = y0 / TILE_PIXELS, ty1 = y1 / TILE_PIXELS;
+                bw = tx1 - tx0 + 1u;
+                c = bw * (ty1 - ty0 + 1u);
+                box = tx0 | (ty0 << 16);
+            }
+        }
+        cnt[e] = c;
+        s_slot[tid * 4 + e] = slot;
+        s_box[tid * 4 + e] = box;
+        s_bw[tid * 4 + e] = (uint16_t)bw;
+        tsum += c;
+    }
+    uint32_t btot;
+    uint32_t off = block_exclusive_scan_256(tsum, s_scan, &btot);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        s_off[tid * 4 + e] = off;
+        off += cnt[e];
+    }
+    if (tid < 32) {
+        if (tid == 0) lb_store(status + tile, lb_pack(epoch, tile == 0 ? LB_INC : LB_AGG, btot));
+        const uint32_t excl = tile == 0 ? 0u : lookback_single(status, tile, epoch, spin_limit, &fc->err);
+        if (tid == 0) {
+            if (tile != 0) lb_store(status + tile, lb_pack(epoch, LB_INC, excl + btot));
+            s_base = excl;
+            if (tile == ntiles - 1) {
+                fc->pairs = excl + btot;
+                if (excl + btot > pair_cap) atomicOr(&fc->err, SPL_DEV_ERR_PAIR_OVERFLOW);
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t gbase = s_base;
+    // load-balanced emission: pair q of this CTA belongs to the last entry whose offset <= q
+    for (uint32_t q = tid; q < btot; q += 256u) {
+        uint32_t lo = 0, hi = BIN_TILE;  // find largest e with s_off[e] <= q (entries with c == 0 share offsets)
+        while (hi - lo > 1u) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_off[mid] <= q) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t li = q - s_off[lo];
+        const uint32_t bw = s_bw[lo], box = s_box[lo];
+        const uint32_t ty = (box >> 16) + li / bw, tx = (box & 0xFFFFu) + li % bw;
+        const uint32_t tid_tile = ty * (uint32_t)tiles_x + tx;
+        const uint32_t g = gbase + q;
+        if (g < pair_cap) {
+            pair_keys[g] = tid_tile;
+            pair_vals[g] = s_slot[lo];
+            atomicAdd(&s_hist[tid_tile & 255u], 1u);
+            atomicAdd(&s_hist[256u + ((tid_tile >> 8) & 255u)], 1u);
+            atomicAdd(&s_hist[512u + ((tid_tile >> 16) & 255u)], 1u);
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < 768u; i += 256u) {
+        const uint32_t v = s_hist[i];
+        if (v) atomicAdd(&fc->hist_pairs[0][0] + i, v);
+    }
+}
+
+void launch_bin(int mode, const uint32_t* order, const float4* rec, FrameCounters* fc, const uint32_t* epoch_word,
+                uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals, uint32_t pair_cap, int tiles_x,
+                uint32_t max_n, uint32_t spin_limit, cudaStream_t st) {
+    const uint32_t grid = max_n == 0 ? 1u : (max_n + BIN_TILE - 1) / BIN_TILE;
+    if (order)
+        k_bin<true><<<grid, 256, 0, st>>>(order, rec, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
+                                          tiles_x, spin_limit);
+    else
+        k_bin<false><<<grid, 256, 0, st>>>(order, rec, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
+                                           tiles_x, spin_limit);
+}
+
+// ------------------------------------------------------------------------------------------------
+__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCounters* __restrict__ fc,
+                              uint32_t pair_cap, uint2* ranges) {
+    const uint32_t P = min(fc->pairs, pair_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        if (i == 0 || keys[i - 1] != k) ranges[k].x = i;
+        if (i + 1 == P || keys[i + 1] != k) ranges[k].y = i + 1;
+    }
+}
+
+void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint32_t pair_cap, uint2* ranges,
+                        cudaStream_t st) {
+    if (pair_cap == 0) return;
+    uint32_t grid = (pair_cap + 255) / 256;
+    if (grid > 152u * 8u) grid = 152u * 8u;
+    k_tile_ranges<<<grid, 256, 0, st>>>(pair_keys, fc, pair_cap, ranges);
+}
+
+// ------------------------------------------------------------------------------------------------
+constexpr int RASTER_BATCH = 256;
+
+template <bool RECT, int BLEND>
+__global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ pair_vals,
+                                                const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
+                                                float psx, float psy, void* __restrict__ out) {
+    __shared__ float4 s_q0[RASTER_BATCH], s_q1[RASTER_BATCH], s_q2[RASTER_BATCH];
+    __shared__ float4 s_q3[RECT ? 1 : RASTER_BATCH];
+    __shared__ float s_lut[256];
+    const uint32_t tid = threadIdx.x;
+    const int tile = blockIdx.x;
+    const int tx = tile % tiles_x, ty = tile / tiles_x;
+    const int px = tx * TILE_PIXELS + (int)(tid & 15u), py = ty * TILE_PIXELS + (int)(tid >> 4);
+    const float X = (float)px + 0.5f, Y = (float)py + 0.5f;
+    s_lut[tid] = (float)tid / 255.0f;
+    const uint2 rg = ranges[tile];
+    const int wy0 = ty * TILE_PIXELS + (int)(tid >> 5) * 2, wy1 = wy0 + 1;
+    const int wx0 = tx * TILE_PIXELS, wx1 = wx0 + TILE_PIXELS - 1;
+    const bool inside = px < W && py < H;
+    bool done = !inside;
+    int cr = 0, cg = 0, cb = 0, ta = 255;
+    float fr = 0.0f, fg = 0.0f, fb = 0.0f, ft = 1.0f;
+    const float alpha_min = 1.0f / 255.0f;
+    for (uint32_t b = rg.x; b < rg.y; b += RASTER_BATCH) {
+        __syncthreads();
+        const uint32_t i = b + tid;
+        if (i < rg.y) {
+            const uint32_t slot = __ldg(pair_vals + i);
+            const float4* r = rec + (size_t)slot * 4;
+            s_q0[tid] = __ldg(r + 0);
+            s_q1[tid] = __ldg(r + 1);
+            s_q2[tid] = __ldg(r + 2);
+            if (!RECT) s_q3[tid] = __ldg(r + 3);
+        }
+        __syncthreads();
+        const uint32_t cnt = min((uint32_t)RASTER_BATCH, rg.y - b);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const float4 q1 = s_q1[j], q2 = s_q2[j];
+            const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
+            const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16), x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
+            if (x1 < wx0 || x0 > wx1 || y1 < wy0 || y0 > wy1) continue;  // warp-uniform
+            if (done || px < x0 || px > x1 || py < y0 || py > y1) continue;
+            const float4 q0 = s_q0[j];
+            const float tcx = fmaf(q0.y, Y, fmaf(q0.x, X, q0.z));
+            const float tcy = fmaf(q1.x, Y, fmaf(q0.w, X, q1.y));
+            if (RECT) {
+                if (!(fabsf(tcx) <= margin && fabsf(tcy) <= margin)) continue;
+            } else {
+                const float4 q3 = s_q3[j];
+                const float dx = fmaf(psx, X, q3.x), dy = fmaf(psy, Y, q3.y);
+                if (!(fabsf(dx) <= q3.z && fabsf(dy) <= q3.z)) continue;
+            }
+            const float power = fmaf(tcx, tcx, tcy * tcy);
+            const float alpha = q1.z * spl_expf(-0.5f * power);
+            if (alpha < alpha_min) continue;
+            const float sr = clamp01(q2.x * alpha), sg = clamp01(q2.y * alpha), sb = clamp01(q2.z * alpha);
+            const float sa = clamp01(alpha);
+            if (BLEND == 0) {
+                const float dA = s_lut[ta];
+                cr = (int)rintf(clamp01(sr * dA + s_lut[cr]) * 255.0f);
+                cg = (int)rintf(clamp01(sg * dA + s_lut[cg]) * 255.0f);
+                cb = (int)rintf(clamp01(sb * dA + s_lut[cb]) * 255.0f);
+                ta = (int)rintf(clamp01(dA * (1.0f - sa)) * 255.0f);
+                done = ta == 0;
+            } else {
+                fr = sr * ft + fr;
+                fg = sg * ft + fg;
+                fb = sb * ft + fb;
+                ft = ft * (1.0f - sa);
+                done = ft < FP32_T_MIN;
+            }
+        }
+        if (__syncthreads_and(done)) break;
+    }
+    if (inside) {
+        const size_t pix = (size_t)py * (size_t)W + (size_t)px;
+        if (BLEND == 0) {
+            reinterpret_cast<uchar4*>(out)[pix] = make_uchar4((unsigned char)cr, (unsigned char)cg, (unsigned char)cb,
+                                                              (unsigned char)ta);
+        } else {
+            reinterpret_cast<float4*>(out)[pix] = make_float4(fr, fg, fb, ft);
+        }
+    }
+}
+
+void launch_raster(bool rect, int blend, const uint2* ranges, const uint32_t* pair_vals, const float4* rec,
+                   const Uniforms& u, void* out, cudaStream_t st) {
+    const int W = (int)u.image_size[0], H = (int)u.image_size[1];
+    const int tiles_x = (W + TILE_PIXELS - 1) / TILE_PIXELS, tiles_y = (H + TILE_PIXELS - 1) / TILE_PIXELS;
+    const int grid = tiles_x * tiles_y;
+    if (grid == 0) return;
+    const float psx = (2.0f * u.view_size[0]) / (float)W;
+    const float psy = -((2.0f * u.view_size[1]) / (float)H);
+    if (rect) {
+        if (blend == 0)
+            k_raster<true, 0><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+        else
+            k_raster<true, 1><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+    } else {
+        if (blend == 0)
+            k_raster<false, 0><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+        else
+            k_raster<false, 1><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+    }
+}
+
+}  // namespace spl

@@ -1,0 +1,250 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle on the same seeded inputs.
+
+Bar: bit-exact depth keys, visible set, sorted permutation, per-splat records and images (FP32 math
+with the WGSL operation order on both sides, and a shared exp method), in every depth-sorting mode,
+both rectangle kinds, both semi-axis methods and both blend targets.
+"""
+import hashlib
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from splatter_gb300 import BlendMode, Configuration, DepthSorting, Renderer, Scene, SplatterError, camera, synthetic
+from splatter_gb300 import _lib
+from tests.helpers import default_cam, image_psnr, oracle_cfg, oracle_uniforms, scene_from_splats60
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 8
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def gpu_frame(cuda, config, records, cam, w, h, splats60=None):
+    import torch
+    r = Renderer(config)
+    n = records.shape[0] if records is not None else splats60.shape[0]
+    s = Scene(r, n)
+    if records is not None:
+        s.load_chunk(records)
+    else:
+        s.write_splats(splats60)
+    img = r.render_frame(s, cam, w, h)
+    torch.cuda.synchronize()
+    keys, idx, info = r.sorted_entries()
+    recs = r.records()
+    torch.cuda.synchronize()
+    out = (img.cpu().numpy(), keys.cpu().numpy().view(np.uint32), idx.cpu().numpy().view(np.uint32), info,
+           recs.cpu().numpy(), s.read_splats())
+    s.close()
+    r.close()
+    return out
+
+
+def oracle_frame(config, sc, cam, w, h):
+    u = oracle_uniforms(oracle, config, cam, w, h)
+    cfg = oracle_cfg(oracle, config)
+    keys, idx, v, nd = oracle.draw_list(u, int(config.depth_sorting), sc["center"])
+    img, st = oracle.render(u, cfg, sc, threads=THREADS)
+    vis_sorted = np.sort(idx)
+    recs, _, _ = oracle.preprocess(u, cfg, sc, vis_sorted, threads=THREADS)
+    return img, keys, idx, v, nd, recs
+
+
+def assert_frame_parity(g, o, config):
+    img, keys, idx, info, recs, _ = g
+    oimg, okeys, oidx, v, nd, orecs = o
+    assert info.visible_count == v
+    assert info.draw_count == nd
+    assert np.array_equal(keys, okeys)
+    assert np.array_equal(idx, oidx)
+    assert np.array_equal(recs.view(np.uint32), orecs.view(np.uint32))
+    if config.blend_mode == BlendMode.UNORM8:
+        assert np.array_equal(img, oimg), f"max |diff| {np.abs(img.astype(int) - oimg.astype(int)).max()}"
+    else:
+        assert np.array_equal(img.view(np.uint32), oimg.view(np.uint32))
+
+
+def test_loader_bit_exact(cuda):
+    rec = synthetic.plain_small(5000, seed=11, sh_order=3)
+    rec[17, 55:58] = (3.0, -30.0, 0.0)  # exercises the clamp around the mean log-scale
+    rec[18, 54] = 120.0  # sigmoid saturates
+    r = Renderer(Configuration(max_splat_count=5000))
+    s = Scene(r, 5000)
+    s.load_chunk(rec)
+    got = s.read_splats()
+    ref = oracle.load_transform(rec)
+    exp60 = synthetic.records_to_splats60(ref["center"], ref["rotation"], ref["scale"], ref["alpha"], ref["sh"])
+    assert np.array_equal(got.view(np.uint32), exp60.view(np.uint32))
+
+
+def test_progressive_chunks_equal_single_load(cuda):
+    rec = synthetic.plain_small(70000, seed=12, sh_order=1)
+    r = Renderer(Configuration(max_splat_count=70000))
+    a = Scene(r, 70000)
+    a.load_chunk(rec)
+    b = Scene(r, 70000)
+    chunk = 16384
+    for c in reversed(range((70000 + chunk - 1) // chunk)):  # showcase.rs:98-103 loads in reverse order
+        b.load_chunk(rec[c * chunk:(c + 1) * chunk], start=c * chunk)
+    assert np.array_equal(a.read_splats(), b.read_splats())
+
+
+def test_load_chunk_file(cuda, tmp_path):
+    rec = synthetic.plain_small(3000, seed=13, sh_order=2)
+    header = ("ply\nformat binary_little_endian 1.0\nelement vertex 3000\n" +
+              "".join(f"property float f{i}\n" for i in range(62)) + "end_header\n").encode()
+    p = tmp_path / "scene.ply"
+    p.write_bytes(header + rec.tobytes())
+    hb, n = Scene.parse_file_header(p)
+    r = Renderer(Configuration(max_splat_count=n))
+    s = Scene(r, n)
+    s.load_chunk_file(p, hb, 1000, 2000)
+    s.load_chunk_file(p, hb, 0, 1000)
+    t = Scene(r, n)
+    t.load_chunk(rec)
+    assert np.array_equal(s.read_splats(), t.read_splats())
+
+
+def test_dev_scene_matches_golden(cuda):
+    import torch
+    g = json.load(open(os.path.join(GOLDEN, "dev_scene.json")))
+    for case in g["cases"]:
+        cfg = Configuration(depth_sorting=DepthSorting(case["depth_sorting"]), spherical_harmonics_order=0,
+                            use_covariance_for_scale=case["covariance"], use_unaligned_rectangles=case["rect"],
+                            field_of_view_y=case["fovy"], max_splat_count=16)
+        r = Renderer(cfg)
+        s = Scene.new_dev_test(r)
+        img = r.render_frame(s, np.array(case["camera"], np.float32), case["width"], case["height"])
+        torch.cuda.synchronize()
+        assert hashlib.sha256(img.cpu().numpy().tobytes()).hexdigest() == case["sha256"], case["name"]
+
+
+MODES = [
+    dict(depth_sorting=DepthSorting.GPU),
+    dict(depth_sorting=DepthSorting.GPU_INDIRECT_DRAW),
+    dict(depth_sorting=DepthSorting.CPU),
+    dict(depth_sorting=DepthSorting.NONE),
+    dict(depth_sorting=DepthSorting.GPU, use_unaligned_rectangles=False),
+    dict(depth_sorting=DepthSorting.GPU, use_covariance_for_scale=False),
+    dict(depth_sorting=DepthSorting.GPU, blend_mode=BlendMode.FP32),
+    dict(depth_sorting=DepthSorting.GPU, spherical_harmonics_order=1, splat_scale=1.7, ellipse_margin=3.0),
+    dict(depth_sorting=DepthSorting.GPU, spherical_harmonics_order=2, frustum_culling_tolerance=1.3,
+         field_of_view_y=math.radians(40)),
+]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=lambda m: "-".join(f"{k}={v}" for k, v in m.items()))
+def test_frame_parity_modes(cuda, mode):
+    n = 30000
+    kw = dict(spherical_harmonics_order=3, max_splat_count=n, field_of_view_y=math.radians(60))
+    kw.update(mode)
+    config = Configuration(**kw)
+    rec = synthetic.plain_small(n, seed=21, sh_order=3)
+    cam = default_cam(dist=7.0)
+    w, h = 320, 240
+    g = gpu_frame(cuda, config, rec, cam, w, h)
+    sc = oracle.load_transform(rec)
+    o = oracle_frame(config, sc, cam, w, h)
+    assert g[3].visible_count > 1000
+    assert_frame_parity(g, o, config)
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 31, 1023, 1024, 1025, 4095, 4096, 4097, 8191, 12289])
+def test_tile_boundaries(cuda, n):
+    config = Configuration(spherical_harmonics_order=1, max_splat_count=max(n, 1), field_of_view_y=math.radians(60))
+    rec = synthetic.plain_small(max(n, 1), seed=100 + n, sh_order=1)[:n]
+    cam = default_cam(dist=6.0)
+    g = gpu_frame(cuda, config, rec, cam, 200, 150)
+    o = oracle_frame(config, oracle.load_transform(rec), cam, 200, 150)
+    assert_frame_parity(g, o, config)
+
+
+def test_everything_culled(cuda):
+    config = Configuration(spherical_harmonics_order=0, max_splat_count=5000)
+    rec = synthetic.plain_small(5000, seed=3)
+    cam = camera.look_at([0.0, 0.0, -50.0], [0.0, 0.0, -100.0])  # looking away from the blob
+    img, keys, idx, info, _, _ = gpu_frame(cuda, config, rec, cam, 64, 48)
+    assert info.visible_count == 0 and info.draw_count == 0 and info.pair_count == 0
+    assert (img == np.array([0, 0, 0, 255], np.uint8)).all()
+
+
+def test_duplicate_positions_keep_index_order(cuda):
+    # equal keys must come out in splat-index order (the stable order of the CPU fallback's sort_by)
+    rec = synthetic.plain_small(20000, seed=31)
+    rec[:, 0:3] = np.round(rec[:, 0:3] * 2) / 2  # many exact duplicates
+    config = Configuration(max_splat_count=20000, spherical_harmonics_order=0)
+    cam = default_cam(dist=9.0)
+    g = gpu_frame(cuda, config, rec, cam, 256, 256)
+    o = oracle_frame(config, oracle.load_transform(rec), cam, 256, 256)
+    assert_frame_parity(g, o, config)
+    keys = g[1]
+    assert np.any(keys[1:] == keys[:-1])
+
+
+@pytest.mark.parametrize("n,bits,distinct", [(1, 32, 1), (100, 8, 3), (4095, 16, 50), (4096, 32, 7),
+                                             (4097, 24, 1000), (100000, 32, 10), (1 << 20, 32, 1 << 30),
+                                             (777777, 16, 300)])
+def test_sort_pairs_stable(cuda, n, bits, distinct):
+    import torch
+    rng = np.random.default_rng(n + bits)
+    keys = (rng.integers(0, distinct, n, dtype=np.int64) * 2654435761 % (1 << 32)).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    r = Renderer(Configuration(max_splat_count=max(n, 1)))
+    kd = torch.from_numpy(keys.view(np.int32)).cuda()
+    vd = torch.from_numpy(vals.view(np.int32)).cuda()
+    ko, vo = r.sort_pairs(kd, vd, key_bits=bits)
+    torch.cuda.synchronize()
+    mask = np.uint32((1 << bits) - 1) if bits < 32 else np.uint32(0xFFFFFFFF)
+    order = np.argsort(keys & mask, kind="stable")
+    assert np.array_equal(vo.cpu().numpy().view(np.uint32), vals[order])
+    assert np.array_equal(ko.cpu().numpy().view(np.uint32), keys[order])
+
+
+def test_lookback_timeout_reports_and_context_survives(cuda):
+    import ctypes
+    import torch
+    lib = _lib.load()
+    flag = ctypes.c_int(0)
+    _lib.check(lib.spl_debug_lookback_timeout(2000, ctypes.byref(flag)))
+    assert flag.value == 1
+    # the context is still usable
+    config = Configuration(max_splat_count=1000, spherical_harmonics_order=0)
+    rec = synthetic.plain_small(1000, seed=5)
+    g = gpu_frame(cuda, config, rec, default_cam(), 64, 64)
+    o = oracle_frame(config, oracle.load_transform(rec), default_cam(), 64, 64)
+    assert_frame_parity(g, o, config)
+    torch.cuda.synchronize()
+
+
+def test_pair_capacity_overflow_is_an_error_not_a_fault(cuda):
+    import torch
+    config = Configuration(max_splat_count=20000, max_pair_count=500, spherical_harmonics_order=0)
+    rec = synthetic.plain_small(20000, seed=8)
+    r = Renderer(config)
+    s = Scene(r, 20000)
+    s.load_chunk(rec)
+    r.render_frame(s, default_cam(dist=6.0), 320, 240)
+    torch.cuda.synchronize()
+    with pytest.raises(SplatterError) as e:
+        r.frame_info()
+    assert e.value.code == _lib.SPL_ERR_CAPACITY
+    info = r.frame_info(check_status=False)
+    assert info.pair_count > 500
+
+
+def test_clustered_1m_1080p_parity(cuda):
+    """Config 'plain path 1M': 1M clustered splats, SH 3, 1920x1080, orbit poses (two of the 32)."""
+    n = 1_000_000
+    config = Configuration(max_splat_count=n, spherical_harmonics_order=3, field_of_view_y=math.radians(60))
+    rec = synthetic.clustered(n, seed=1)
+    sc = oracle.load_transform(rec)
+    poses = camera.orbit_poses(32, seed=7, radius=(6.0, 12.0))
+    for cam in (poses[0], poses[13]):
+        g = gpu_frame(cuda, config, rec, cam, 1920, 1080)
+        o = oracle_frame(config, sc, cam, 1920, 1080)
+        assert_frame_parity(g, o, config)
+        assert image_psnr(g[0], o[0]) == float("inf")

@@ -172,6 +172,21 @@ SPL_API int spl_scene_read_splats(const spl_scene* s, float* splats60, uint64_t 
 SPL_API int spl_sort_pairs(spl_renderer* r, const uint32_t* keys_in, const uint32_t* values_in, uint32_t* keys_out,
                    uint32_t* values_out, uint64_t count, uint32_t key_bits, void* stream);
 
+/* ---- sorting without allocation -------------------------------------------------------------------- */
+/* No counterpart in the reference: an addition for callers that cannot allocate device memory when
+ * they sort — hosts that give all device memory to their own pool up front, code running while a
+ * CUDA graph is captured, plug-ins that may only touch the buffers they are handed.
+ * spl_sort_pairs_no_alloc is spl_sort_pairs (same stable result, same kernels) without a renderer:
+ * its scratch is a static device array the library reserves on every device that loads it (2.6 MB,
+ * held until the process exits), and it calls no allocator.  At most SPL_NO_ALLOC_MAX_PAIRS pairs
+ * per call (larger counts return SPL_ERR_INVALID).  All calls on a device share that scratch: calls
+ * whose GPU work overlaps race and give wrong results, so order them on one stream.  The first call
+ * on a device looks up the scratch address (cudaGetSymbolAddress); make it before any stream
+ * capture.  Inputs and outputs must not overlap.  Asynchronous on `stream`. */
+#define SPL_NO_ALLOC_MAX_PAIRS 262144u
+SPL_API int spl_sort_pairs_no_alloc(const uint32_t* keys_in, const uint32_t* values_in, uint32_t* keys_out,
+                                    uint32_t* values_out, uint64_t count, uint32_t key_bits, void* stream);
+
 /* ---- diagnostics ----------------------------------------------------------------------------------- */
 /* Stage timing with CUDA events on the launching streams (off by default).  When enabled, each
  * render_frame records events around its stages; spl_renderer_stage_times waits for the last frame

@@ -86,7 +86,10 @@ SIGNATURES = [
     ("spl_renderer_set_profiling", I32, [P, I32]),
     ("spl_renderer_stage_times", I32, [P, ctypes.POINTER(ctypes.c_float), I32]),
     ("spl_renderer_launches_per_frame", I32, [P, U32, U32]),
+    ("spl_sort_pairs_no_alloc", I32, [P, P, P, P, U64, U32, P]),
 ]
+
+NO_ALLOC_MAX_PAIRS = 262144
 
 STAGES = ["cull", "preprocess", "depth_sort", "bin", "pair_sort", "ranges", "raster", "frame"]
 

@@ -67,6 +67,17 @@ uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
 
 }  // namespace
 
+// Error reporting for the other translation units of the library.
+int spl_internal_fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
 // Frame uniforms (renderer.rs:364-409; utils.rs:45-70).  The camera is the camera-to-world matrix
 // (motor3d_to_mat4 of the motor, utils.rs:31-42); the view matrix is its rigid inverse (the
 // reference inverts the motor, renderer.rs:365).  field_of_view_y is a documented extension (the

@@ -32,7 +32,7 @@ def test_every_declared_symbol_is_exported(lib):
     for n in names:
         assert hasattr(lib, n), n
     bound = {s[0] for s in _lib.SIGNATURES}
-    assert set(names) <= bound | {"spl_scene_create_no_alloc"} or set(names) == bound
+    assert set(names) == bound
 
 
 def test_config_default_is_showcase_literal(lib):

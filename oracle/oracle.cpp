@@ -400,8 +400,10 @@ bool preprocess_one(const OU& u, const OCfg& cfg, const float* center, const flo
     }
     const F cxp = (Zx + vw) / sx, exp_ = ex / sx;
     const F cyp = (Zy - vh) / sy, eyp = ey / (-sy);
-    const F fx0 = std::floor(cxp - exp_) - F(1), fx1 = std::ceil(cxp + exp_) + F(1);
-    const F fy0 = std::floor(cyp - eyp) - F(1), fy1 = std::ceil(cyp + eyp) + F(1);
+    // pixels whose centre (p + 0.5) lies in the exact box, widened by 1/64 px against rounding
+    const F eps = (F)0.015625f;
+    const F fx0 = std::ceil(((cxp - exp_) - eps) - F(0.5)), fx1 = std::floor(((cxp + exp_) + eps) - F(0.5));
+    const F fy0 = std::ceil(((cyp - eyp) - eps) - F(0.5)), fy1 = std::floor(((cyp + eyp) + eps) - F(0.5));
     const F al = (F)alpha;
     bool ok = std::isfinite(A00) && std::isfinite(A01) && std::isfinite(B0) && std::isfinite(A10) &&
               std::isfinite(A11) && std::isfinite(B1) && std::isfinite(rgb[0]) && std::isfinite(rgb[1]) &&

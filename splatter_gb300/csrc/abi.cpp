@@ -127,43 +127,33 @@ struct spl_renderer {
     uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr, *idx = nullptr;
     float4* rec = nullptr;
     uint64_t* st_cull = nullptr;  // [ceil(max_n/4096)]
-    uint64_t* st_sort = nullptr;  // [4][ceil(max_n/4096) * 256]
     uint64_t* st_bin = nullptr;   // [ceil(max_n/1024)]
     uint32_t *pk_a = nullptr, *pk_b = nullptr, *pv_a = nullptr, *pv_b = nullptr;
-    uint64_t* st_pairs = nullptr;  // [3][ceil(pair_cap/4096) * 256]
     FrameCounters* fc = nullptr;
     FrameCounters* fc_sort = nullptr;  // counters of spl_sort_pairs
+    uint32_t* coop_cnt = nullptr;      // [256][sort_coop_grid()] digit counts of the cooperative sort
     uint32_t* epoch = nullptr;
     FrameCounters* host_fc = nullptr;  // pinned
     uint2* ranges = nullptr;
     uint64_t ranges_cap = 0;
-    cudaStream_t aux = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // last frame
     cudaStream_t last_stream = nullptr;
     bool has_frame = false;
     uint32_t last_w = 0, last_h = 0;
     uint64_t last_n = 0;
     const uint32_t* final_pair_vals = nullptr;
-    // stage profiling: events 0..8 on the main stream, 9..10 on the side stream
+    // stage profiling: events 0..7 on the frame's stream
     bool profiling = false;
-    cudaEvent_t ev_prof[11] = {};
+    cudaEvent_t ev_prof[8] = {};
 
-    uint64_t sort_tiles() const { return ceil_div(max_n, SORT_TILE); }
-    uint64_t pair_tiles() const { return ceil_div(pair_cap, SORT_TILE); }
 
     void release() {
         dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec);
-        dfree(st_cull); dfree(st_sort); dfree(st_bin);
-        dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b); dfree(st_pairs);
-        dfree(fc); dfree(fc_sort); dfree(epoch); dfree(ranges);
+        dfree(st_cull); dfree(st_bin);
+        dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b);
+        dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges);
         if (host_fc) cudaFreeHost(host_fc);
         host_fc = nullptr;
-        if (aux) cudaStreamDestroy(aux);
-        if (ev_fork) cudaEventDestroy(ev_fork);
-        if (ev_join) cudaEventDestroy(ev_join);
-        aux = nullptr;
-        ev_fork = ev_join = nullptr;
         for (auto& e : ev_prof) {
             if (e) cudaEventDestroy(e);
             e = nullptr;
@@ -332,8 +322,6 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
     }
     r->pair_cap = pc;
     const uint64_t n = r->max_n;
-    const uint64_t st_sort_words = 4 * r->sort_tiles() * 256;
-    const uint64_t st_pair_words = 3 * r->pair_tiles() * 256;
 #define TRY(x)           \
     do {                 \
         rc = (x);        \
@@ -350,30 +338,24 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
     TRY(dalloc(&r->idx, n));
     TRY(dalloc(&r->rec, n * 4));
     TRY(dalloc(&r->st_cull, ceil_div(n, CULL_TILE)));
-    TRY(dalloc(&r->st_sort, st_sort_words));
     TRY(dalloc(&r->st_bin, ceil_div(n, BIN_TILE)));
     TRY(dalloc(&r->pk_a, pc));
     TRY(dalloc(&r->pk_b, pc));
     TRY(dalloc(&r->pv_a, pc));
     TRY(dalloc(&r->pv_b, pc));
-    TRY(dalloc(&r->st_pairs, st_pair_words));
     TRY(dalloc(&r->fc, 1));
     TRY(dalloc(&r->fc_sort, 1));
     TRY(dalloc(&r->epoch, 1));
+    TRY(dalloc(&r->coop_cnt, 256 * (size_t)sort_coop_grid()));
 #undef TRY
     cudaError_t e = cudaSuccess;
     // status words start at epoch 0, which no frame uses
     if (e == cudaSuccess) e = cudaMemset(r->st_cull, 0, ceil_div(n, CULL_TILE) * 8);
-    if (e == cudaSuccess) e = cudaMemset(r->st_sort, 0, st_sort_words * 8);
     if (e == cudaSuccess) e = cudaMemset(r->st_bin, 0, ceil_div(n, BIN_TILE) * 8);
-    if (e == cudaSuccess) e = cudaMemset(r->st_pairs, 0, st_pair_words * 8);
     if (e == cudaSuccess) e = cudaMemset(r->fc, 0, sizeof(FrameCounters));
     if (e == cudaSuccess) e = cudaMemset(r->fc_sort, 0, sizeof(FrameCounters));
     if (e == cudaSuccess) e = cudaMemset(r->epoch, 0, 4);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->host_fc), sizeof(FrameCounters));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->aux, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -428,52 +410,28 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     launch_frame_begin(r->fc, r->epoch, st);
     launch_cull_key(mode, sv, u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
     r->mark(1, st);
-    // vertex stage on the side stream, overlapping the depth sort
-    CU(cudaEventRecord(r->ev_fork, st));
-    CU(cudaStreamWaitEvent(r->aux, r->ev_fork, 0));
-    r->mark(9, r->aux);
     launch_preprocess((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
-                      cfg.use_unaligned_rectangles != 0, sv, u, r->idx, r->fc, r->rec, N, r->aux);
-    r->mark(10, r->aux);
-    CU(cudaEventRecord(r->ev_join, r->aux));
+                      cfg.use_unaligned_rectangles != 0, sv, u, r->idx, r->fc, r->rec, N, st);
+    r->mark(2, st);
     const uint32_t* order = nullptr;
     if (mode != DS_NONE && N > 0) {
-        // four stable 8-bit passes: a -> b -> a -> b -> a; pass 0 takes the compaction slot as value
-        uint32_t* src_k = r->keys_a;
-        const uint32_t* src_v = nullptr;
-        uint32_t* dst_k = r->keys_b;
-        uint32_t* dst_v = r->vals_b;
-        const uint64_t stride = r->sort_tiles() * 256;
-        for (int p = 0; p < 4; ++p) {
-            launch_onesweep(src_k, src_v, dst_k, dst_v, &r->fc->visible, N, r->fc->hist_depth[p],
-                            r->st_sort + p * stride, &r->fc->tile_counter[1 + p], r->epoch, 8 * p, sl, &r->fc->err,
-                            st);
-            uint32_t* next_k = dst_k == r->keys_b ? r->keys_a : r->keys_b;
-            uint32_t* next_v = dst_v == r->vals_b ? r->vals_a : r->vals_b;
-            src_k = dst_k;
-            src_v = dst_v;
-            dst_k = next_k;
-            dst_v = next_v;
-        }
-        order = src_v;  // == vals_a, keys in keys_a
+        // four stable 8-bit passes a -> b -> a -> b -> a in one cooperative launch; pass 0 takes the
+        // compaction slot as the value
+        CU(launch_sort_coop(r->keys_a, r->keys_b, r->vals_a, r->vals_b, true, &r->fc->visible, N, 4, 0, r->coop_cnt,
+                            r->fc->barrier, sl, &r->fc->err, st));
+        order = r->vals_a;  // keys in keys_a
     }
-    r->mark(2, st);
-    CU(cudaStreamWaitEvent(st, r->ev_join, 0));
-    CU(cudaMemsetAsync(r->ranges, 0, tiles * sizeof(uint2), st));
     r->mark(3, st);
+    CU(cudaMemsetAsync(r->ranges, 0, tiles * sizeof(uint2), st));
     launch_bin(mode, order, r->rec, r->fc, r->epoch, r->st_bin, r->pk_a, r->pv_a, (uint32_t)r->pair_cap,
                (int)tiles_x, N, sl, st);
     r->mark(4, st);
     // stable sort of the pairs by tile id keeps each tile's list in depth order
     const int passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
-    uint32_t *pk = r->pk_a, *pv = r->pv_a, *qk = r->pk_b, *qv = r->pv_b;
-    const uint64_t pstride = r->pair_tiles() * 256;
-    for (int p = 0; p < passes; ++p) {
-        launch_onesweep(pk, pv, qk, qv, &r->fc->pairs, (uint32_t)r->pair_cap, r->fc->hist_pairs[p],
-                        r->st_pairs + p * pstride, &r->fc->tile_counter[5 + p], r->epoch, 8 * p, sl, &r->fc->err, st);
-        std::swap(pk, qk);
-        std::swap(pv, qv);
-    }
+    CU(launch_sort_coop(r->pk_a, r->pk_b, r->pv_a, r->pv_b, false, &r->fc->pairs, (uint32_t)r->pair_cap, passes, 0,
+                        r->coop_cnt, r->fc->barrier, sl, &r->fc->err, st));
+    const uint32_t* pk = (passes & 1) ? r->pk_b : r->pk_a;
+    const uint32_t* pv = (passes & 1) ? r->pv_b : r->pv_a;
     r->mark(5, st);
     launch_tile_ranges(pk, r->fc, (uint32_t)r->pair_cap, r->ranges, st);
     r->mark(6, st);
@@ -503,11 +461,10 @@ int spl_renderer_stage_times(spl_renderer* r, float* ms, int count) {
     if (!r || !ms || count < SPL_STAGE_COUNT) return fail(SPL_ERR_INVALID, "need %d outputs", SPL_STAGE_COUNT);
     if (!r->profiling || !r->has_frame) return fail(SPL_ERR_INVALID, "profiling is off or no frame rendered");
     CU(cudaEventSynchronize(r->ev_prof[7]));
-    CU(cudaEventSynchronize(r->ev_prof[10]));
     auto el = [&](int a, int b, float* out) -> cudaError_t { return cudaEventElapsedTime(out, r->ev_prof[a], r->ev_prof[b]); };
     CU(el(0, 1, &ms[SPL_STAGE_CULL]));
-    CU(el(9, 10, &ms[SPL_STAGE_PREPROCESS]));
-    CU(el(1, 2, &ms[SPL_STAGE_DEPTH_SORT]));
+    CU(el(1, 2, &ms[SPL_STAGE_PREPROCESS]));
+    CU(el(2, 3, &ms[SPL_STAGE_DEPTH_SORT]));
     CU(el(3, 4, &ms[SPL_STAGE_BIN]));
     CU(el(4, 5, &ms[SPL_STAGE_PAIR_SORT]));
     CU(el(5, 6, &ms[SPL_STAGE_RANGES]));
@@ -519,10 +476,11 @@ int spl_renderer_stage_times(spl_renderer* r, float* ms, int count) {
 int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint32_t height) {
     if (!r) return 0;
     const uint64_t tiles = ceil_div(width, TILE_PIXELS) * ceil_div(height, TILE_PIXELS);
-    const int pair_passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
-    const int depth_passes = r->cfg.depth_sorting == DS_NONE ? 0 : 4;
-    // frame_begin, cull, preprocess, depth passes, ranges memset, bin, pair passes, ranges, raster
-    return 1 + 1 + 1 + depth_passes + 1 + 1 + pair_passes + 1 + 1;
+    (void)tiles;
+    const int depth_sort = r->cfg.depth_sorting == DS_NONE ? 0 : 1;
+    // frame_begin, cull, preprocess, depth sort (one cooperative launch), ranges memset, bin,
+    // pair sort (one cooperative launch), ranges, raster
+    return 1 + 1 + 1 + depth_sort + 1 + 1 + 1 + 1 + 1;
 }
 
 int spl_renderer_frame_info(spl_renderer* r, spl_frame_info* info) {
@@ -576,21 +534,14 @@ int spl_sort_pairs(spl_renderer* r, const uint32_t* keys_in, const uint32_t* val
     const int passes = (int)(key_bits / 8);
     launch_frame_begin(r->fc_sort, r->epoch, st);
     launch_set_count(&r->fc_sort->visible, (uint32_t)count, st);
-    launch_histogram(keys_in, &r->fc_sort->visible, (uint32_t)count, r->fc_sort->hist_depth[0], st);
-    const uint64_t stride = r->sort_tiles() * 256;
-    const uint32_t* kin = keys_in;
-    const uint32_t* vin = values_in;
-    for (int p = 0; p < passes; ++p) {
-        const bool to_out = ((passes - 1 - p) % 2) == 0;
-        uint32_t* kout = to_out ? keys_out : r->keys_b;
-        uint32_t* vout = to_out ? values_out : r->vals_b;
-        launch_onesweep(kin, vin, kout, vout, &r->fc_sort->visible, (uint32_t)count, r->fc_sort->hist_depth[p],
-                        r->st_sort + p * stride, &r->fc_sort->tile_counter[1 + p], r->epoch, 8 * p, r->spin_limit,
-                        &r->fc_sort->err, st);
-        kin = kout;
-        vin = vout;
-    }
-    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(r->keys_a, keys_in, count * 4, cudaMemcpyDeviceToDevice, st));
+    CU(cudaMemcpyAsync(r->vals_a, values_in, count * 4, cudaMemcpyDeviceToDevice, st));
+    CU(launch_sort_coop(r->keys_a, r->keys_b, r->vals_a, r->vals_b, false, &r->fc_sort->visible, (uint32_t)count,
+                        passes, 0, r->coop_cnt, r->fc_sort->barrier, r->spin_limit, &r->fc_sort->err, st));
+    const uint32_t* kr = (passes & 1) ? r->keys_b : r->keys_a;
+    const uint32_t* vr = (passes & 1) ? r->vals_b : r->vals_a;
+    CU(cudaMemcpyAsync(keys_out, kr, count * 4, cudaMemcpyDeviceToDevice, st));
+    CU(cudaMemcpyAsync(values_out, vr, count * 4, cudaMemcpyDeviceToDevice, st));
     return SPL_OK;
 }
 

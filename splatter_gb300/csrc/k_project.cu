@@ -395,8 +395,10 @@ __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, con
         }
         const float cxp = (t0 + vw) / psx, exq = ex / psx;
         const float cyp = (t1 - vh) / psy, eyq = ey / (-psy);
-        const float fx0 = floorf(cxp - exq) - 1.0f, fx1 = ceilf(cxp + exq) + 1.0f;
-        const float fy0 = floorf(cyp - eyq) - 1.0f, fy1 = ceilf(cyp + eyq) + 1.0f;
+        // pixels whose centre (p + 0.5) lies in the exact box, widened by 1/64 px against rounding
+        const float eps = 0.015625f;
+        const float fx0 = ceilf(((cxp - exq) - eps) - 0.5f), fx1 = floorf(((cxp + exq) + eps) - 0.5f);
+        const float fy0 = ceilf(((cyp - eyq) - eps) - 0.5f), fy1 = floorf(((cyp + eyq) + eps) - 0.5f);
         const float al = sca.w;
         bool ok = isfinite(A00) && isfinite(A01) && isfinite(B0) && isfinite(A10) && isfinite(A11) && isfinite(B1) &&
                   isfinite(cr) && isfinite(cg) && isfinite(cb) && isfinite(fx0) && isfinite(fx1) && isfinite(fy0) &&

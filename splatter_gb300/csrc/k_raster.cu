@@ -162,6 +162,13 @@ void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint
 // ------------------------------------------------------------------------------------------------
 constexpr int RASTER_BATCH = 256;
 
+// One CTA per 16x16 tile, one thread per pixel; warp w owns the 16x2 strip of rows 2w, 2w+1.  The
+// tile's records (depth order) are staged through shared memory in batches of 256.  For each batch a
+// warp first builds its relevance list with ballots (32 box tests per instruction slot, in order),
+// then evaluates only the records whose pixel box meets its strip.  Per pixel: box test, coverage
+// test, falloff, 1/255 discard, blend — the same operations as the oracle's raster_tile, so the
+// image is bit-identical.  A warp whose pixels are all finished skips the rest of the list, and the
+// CTA stops once every pixel is finished (T == 0 in unorm8 mode, T < 1e-4 in fp32 mode).
 template <bool RECT, int BLEND>
 __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ pair_vals,
                                                 const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
@@ -169,7 +176,7 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     __shared__ float4 s_q0[RASTER_BATCH], s_q1[RASTER_BATCH], s_q2[RASTER_BATCH];
     __shared__ float4 s_q3[RECT ? 1 : RASTER_BATCH];
     __shared__ float s_lut[256];
-    const uint32_t tid = threadIdx.x;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
     const int tile = blockIdx.x;
     const int tx = tile % tiles_x, ty = tile / tiles_x;
     const int px = tx * TILE_PIXELS + (int)(tid & 15u), py = ty * TILE_PIXELS + (int)(tid >> 4);
@@ -180,6 +187,7 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     const int wx0 = tx * TILE_PIXELS, wx1 = wx0 + TILE_PIXELS - 1;
     const bool inside = px < W && py < H;
     bool done = !inside;
+    bool warp_done = __all_sync(FULL_MASK, done);
     int cr = 0, cg = 0, cb = 0, ta = 255;
     float fr = 0.0f, fg = 0.0f, fb = 0.0f, ft = 1.0f;
     const float alpha_min = 1.0f / 255.0f;
@@ -196,41 +204,58 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
         }
         __syncthreads();
         const uint32_t cnt = min((uint32_t)RASTER_BATCH, rg.y - b);
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const float4 q1 = s_q1[j], q2 = s_q2[j];
-            const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
-            const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16), x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
-            if (x1 < wx0 || x0 > wx1 || y1 < wy0 || y0 > wy1) continue;  // warp-uniform
-            if (done || px < x0 || px > x1 || py < y0 || py > y1) continue;
-            const float4 q0 = s_q0[j];
-            const float tcx = fmaf(q0.y, Y, fmaf(q0.x, X, q0.z));
-            const float tcy = fmaf(q1.x, Y, fmaf(q0.w, X, q1.y));
-            if (RECT) {
-                if (!(fabsf(tcx) <= margin && fabsf(tcy) <= margin)) continue;
-            } else {
-                const float4 q3 = s_q3[j];
-                const float dx = fmaf(psx, X, q3.x), dy = fmaf(psy, Y, q3.y);
-                if (!(fabsf(dx) <= q3.z && fabsf(dy) <= q3.z)) continue;
+        if (!warp_done) {
+            for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
+                bool rel = false;
+                const uint32_t jl = j0 + lane;
+                if (jl < cnt) {
+                    const uint32_t lo = __float_as_uint(s_q1[jl].w), hi = __float_as_uint(s_q2[jl].w);
+                    rel = !((int)(hi & 0xFFFFu) < wx0 || (int)(lo & 0xFFFFu) > wx1 || (int)(hi >> 16) < wy0 ||
+                            (int)(lo >> 16) > wy1);
+                }
+                uint32_t mask = __ballot_sync(FULL_MASK, rel);
+                while (mask) {
+                    const uint32_t j = j0 + (uint32_t)(__ffs(mask) - 1);
+                    mask &= mask - 1u;
+                    const float4 q1 = s_q1[j], q2 = s_q2[j];
+                    const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
+                    const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
+                    const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
+                    if (done || (unsigned)(px - x0) > (unsigned)(x1 - x0) || (unsigned)(py - y0) > (unsigned)(y1 - y0))
+                        continue;
+                    const float4 q0 = s_q0[j];
+                    const float tcx = fmaf(q0.y, Y, fmaf(q0.x, X, q0.z));
+                    const float tcy = fmaf(q1.x, Y, fmaf(q0.w, X, q1.y));
+                    if (RECT) {
+                        if (!(fabsf(tcx) <= margin && fabsf(tcy) <= margin)) continue;
+                    } else {
+                        const float4 q3 = s_q3[j];
+                        const float dx = fmaf(psx, X, q3.x), dy = fmaf(psy, Y, q3.y);
+                        if (!(fabsf(dx) <= q3.z && fabsf(dy) <= q3.z)) continue;
+                    }
+                    const float power = fmaf(tcx, tcx, tcy * tcy);
+                    const float alpha = q1.z * spl_expf_nonpos(-0.5f * power);
+                    if (alpha < alpha_min) continue;
+                    // __saturatef == clamp to [0, 1] (NaN -> 0); __float2int_rn == (int)rintf
+                    const float sr = __saturatef(q2.x * alpha), sg = __saturatef(q2.y * alpha);
+                    const float sb = __saturatef(q2.z * alpha), sa = __saturatef(alpha);
+                    if (BLEND == 0) {
+                        const float dA = s_lut[ta];
+                        cr = __float2int_rn(__saturatef(sr * dA + s_lut[cr]) * 255.0f);
+                        cg = __float2int_rn(__saturatef(sg * dA + s_lut[cg]) * 255.0f);
+                        cb = __float2int_rn(__saturatef(sb * dA + s_lut[cb]) * 255.0f);
+                        ta = __float2int_rn(__saturatef(dA * (1.0f - sa)) * 255.0f);
+                        done = ta == 0;
+                    } else {
+                        fr = sr * ft + fr;
+                        fg = sg * ft + fg;
+                        fb = sb * ft + fb;
+                        ft = ft * (1.0f - sa);
+                        done = ft < FP32_T_MIN;
+                    }
+                }
             }
-            const float power = fmaf(tcx, tcx, tcy * tcy);
-            const float alpha = q1.z * spl_expf(-0.5f * power);
-            if (alpha < alpha_min) continue;
-            const float sr = clamp01(q2.x * alpha), sg = clamp01(q2.y * alpha), sb = clamp01(q2.z * alpha);
-            const float sa = clamp01(alpha);
-            if (BLEND == 0) {
-                const float dA = s_lut[ta];
-                cr = (int)rintf(clamp01(sr * dA + s_lut[cr]) * 255.0f);
-                cg = (int)rintf(clamp01(sg * dA + s_lut[cg]) * 255.0f);
-                cb = (int)rintf(clamp01(sb * dA + s_lut[cb]) * 255.0f);
-                ta = (int)rintf(clamp01(dA * (1.0f - sa)) * 255.0f);
-                done = ta == 0;
-            } else {
-                fr = sr * ft + fr;
-                fg = sg * ft + fg;
-                fb = sb * ft + fb;
-                ft = ft * (1.0f - sa);
-                done = ft < FP32_T_MIN;
-            }
+            warp_done = __all_sync(FULL_MASK, done);
         }
         if (__syncthreads_and(done)) break;
     }

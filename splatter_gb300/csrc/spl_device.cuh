@@ -132,6 +132,24 @@ __device__ __forceinline__ float spl_expf(float x) {
     return __fmul_rn(__fmul_rn(p, s1), s2);
 }
 
+// spl_expf restricted to finite x <= 0 (the fragment falloff): the same result bit for bit.  For
+// n >= -125 the two-factor scaling reduces to one multiply by 2^n, exact because p * 2^n is normal.
+__device__ __forceinline__ float spl_expf_nonpos(float x) {
+    if (x < -87.0f) return spl_expf(x);
+    const float n = rintf(__fmul_rn(x, 1.44269502162933349609375f));
+    float r = fmaf(n, -0.693145751953125f, x);
+    r = fmaf(n, -1.428606765330187045e-06f, r);
+    float p = 1.98412698412698412e-04f;
+    p = fmaf(p, r, 1.38888888888888889e-03f);
+    p = fmaf(p, r, 8.33333333333333333e-03f);
+    p = fmaf(p, r, 4.16666666666666667e-02f);
+    p = fmaf(p, r, 1.66666666666666667e-01f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
+}
+
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 
 // WGSL u32(f32): truncate, saturate, NaN -> 0.

@@ -37,7 +37,7 @@ struct FrameCounters {
     uint32_t err;              // SPL_DEV_ERR_* bits
     uint32_t draw;             // entries drawn (mode dependent)
     uint32_t epoch;            // copy of the frame epoch (for readback)
-    uint32_t pad[2];
+    uint32_t barrier[2];       // grid barrier of the cooperative sort: arrivals, generation
     uint32_t hist_depth[4][256];  // digit histograms of the visible depth keys
     uint32_t hist_pairs[3][256];  // digit histograms of the tile ids of all pairs
 };
@@ -93,6 +93,12 @@ void launch_splats60_to_soa(const float* s60, uint32_t count, float* x, float* y
 void launch_soa_to_splats60(const SceneView& s, uint32_t start, uint32_t count, float* s60, cudaStream_t st);
 void launch_gather_entries(const uint32_t* keys, const uint32_t* slots, const uint32_t* idx, const FrameCounters* fc,
                            int mode, uint32_t* keys_out, uint32_t* idx_out, uint32_t cap, cudaStream_t st);
+// All passes of a stable LSD radix sort in one cooperative launch (k_sort_coop.cu).  Pass p reads
+// buffers (p even: 0, odd: 1) and writes the other; cnt holds 256 x sort_coop_grid() words.
+cudaError_t launch_sort_coop(uint32_t* keys0, uint32_t* keys1, uint32_t* vals0, uint32_t* vals1, bool iota_first,
+                             const uint32_t* n_ptr, uint32_t n_cap, int passes, int shift0, uint32_t* cnt,
+                             uint32_t* bar, uint32_t spin_limit, uint32_t* err, cudaStream_t st);
+int sort_coop_grid();
 void launch_histogram(const uint32_t* keys, const uint32_t* n_ptr, uint32_t n_cap, uint32_t* hist4x256,
                       cudaStream_t st);
 void launch_set_count(uint32_t* dst, uint32_t value, cudaStream_t st);

@@ -150,7 +150,7 @@ def stage_bytes(stage, V, D, P, N, W, H, sh_order=3):
     if stage == "cull":
         return 12 * N + 8 * V                       # x,y,z read; (key, index) written per visible splat
     if stage == "preprocess":
-        return (4 + 12 + 16 + 16 + shb + 64) * V    # index, centre, rotation, scale+alpha, SH; 64-B record
+        return (4 + 12 + 16 + 16 + shb + 64 + 8) * V  # index, centre, rotation, scale+alpha, SH; record + box
     if stage == "depth_sort":
         return (12 + 3 * 16) * V                    # 4 passes: read key(+value), write key+value
     if stage == "bin":

@@ -126,12 +126,13 @@ struct spl_renderer {
     // depth sort: K1 writes keys_a/idx; 4 passes a->b->a->b->a leave (key, slot) in keys_a/vals_a
     uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr, *idx = nullptr;
     float4* rec = nullptr;
+    uint2* boxes = nullptr;  // pixel box of each record, for the binning kernel
     uint64_t* st_cull = nullptr;  // [ceil(max_n/4096)]
     uint64_t* st_bin = nullptr;   // [ceil(max_n/1024)]
     uint32_t *pk_a = nullptr, *pk_b = nullptr, *pv_a = nullptr, *pv_b = nullptr;
     FrameCounters* fc = nullptr;
     FrameCounters* fc_sort = nullptr;  // counters of spl_sort_pairs
-    uint32_t* coop_cnt = nullptr;      // [256][sort_coop_grid()] digit counts of the cooperative sort
+    uint32_t* coop_cnt = nullptr;      // [256][grid, padded to 4] digit counts + [256] totals (cooperative sort)
     uint32_t* epoch = nullptr;
     FrameCounters* host_fc = nullptr;  // pinned
     uint2* ranges = nullptr;
@@ -148,7 +149,7 @@ struct spl_renderer {
 
 
     void release() {
-        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec);
+        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes);
         dfree(st_cull); dfree(st_bin);
         dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b);
         dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges);
@@ -337,6 +338,7 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
     TRY(dalloc(&r->vals_b, n));
     TRY(dalloc(&r->idx, n));
     TRY(dalloc(&r->rec, n * 4));
+    TRY(dalloc(&r->boxes, n));
     TRY(dalloc(&r->st_cull, ceil_div(n, CULL_TILE)));
     TRY(dalloc(&r->st_bin, ceil_div(n, BIN_TILE)));
     TRY(dalloc(&r->pk_a, pc));
@@ -346,7 +348,7 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
     TRY(dalloc(&r->fc, 1));
     TRY(dalloc(&r->fc_sort, 1));
     TRY(dalloc(&r->epoch, 1));
-    TRY(dalloc(&r->coop_cnt, 256 * (size_t)sort_coop_grid()));
+    TRY(dalloc(&r->coop_cnt, 256 * (((size_t)sort_coop_grid() + 3) & ~(size_t)3) + 256));
 #undef TRY
     cudaError_t e = cudaSuccess;
     // status words start at epoch 0, which no frame uses
@@ -354,6 +356,8 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
     if (e == cudaSuccess) e = cudaMemset(r->st_bin, 0, ceil_div(n, BIN_TILE) * 8);
     if (e == cudaSuccess) e = cudaMemset(r->fc, 0, sizeof(FrameCounters));
     if (e == cudaSuccess) e = cudaMemset(r->fc_sort, 0, sizeof(FrameCounters));
+    if (e == cudaSuccess)
+        e = cudaMemset(r->coop_cnt, 0, (256 * (((size_t)sort_coop_grid() + 3) & ~(size_t)3) + 256) * 4);
     if (e == cudaSuccess) e = cudaMemset(r->epoch, 0, 4);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->host_fc), sizeof(FrameCounters));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -411,7 +415,7 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     launch_cull_key(mode, sv, u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
     r->mark(1, st);
     launch_preprocess((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
-                      cfg.use_unaligned_rectangles != 0, sv, u, r->idx, r->fc, r->rec, N, st);
+                      cfg.use_unaligned_rectangles != 0, sv, u, r->idx, r->fc, r->rec, r->boxes, N, st);
     r->mark(2, st);
     const uint32_t* order = nullptr;
     if (mode != DS_NONE && N > 0) {
@@ -423,7 +427,7 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     }
     r->mark(3, st);
     CU(cudaMemsetAsync(r->ranges, 0, tiles * sizeof(uint2), st));
-    launch_bin(mode, order, r->rec, r->fc, r->epoch, r->st_bin, r->pk_a, r->pv_a, (uint32_t)r->pair_cap,
+    launch_bin(mode, order, r->boxes, r->fc, r->epoch, r->st_bin, r->pk_a, r->pv_a, (uint32_t)r->pair_cap,
                (int)tiles_x, N, sl, st);
     r->mark(4, st);
     // stable sort of the pairs by tile id keeps each tile's list in depth order

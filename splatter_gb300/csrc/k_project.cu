@@ -312,7 +312,8 @@ __device__ __forceinline__ float sh_channel(const float* sh, int c, float x, flo
 
 template <int SHO, bool COV, bool RECT>
 __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
-                                                    const FrameCounters* __restrict__ fc, float4* __restrict__ rec) {
+                                                    const FrameCounters* __restrict__ fc, float4* __restrict__ rec,
+                                                    uint2* __restrict__ boxes) {
     const uint32_t V = fc->visible;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < V; slot += gridDim.x * blockDim.x) {
         const uint32_t i = __ldg(idx + slot);
@@ -417,37 +418,39 @@ __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, con
         o[1] = make_float4(A11, B1, al, __uint_as_float(lo));
         o[2] = make_float4(cr, cg, cb, __uint_as_float(hi));
         o[3] = RECT ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : make_float4(bx, by, R, 0.0f);
+        boxes[slot] = make_uint2(lo, hi);  // compact copy for the binning kernel
     }
 }
 
 template <int SHO, bool COV>
 static void launch_pre2(bool rect, dim3 g, const SceneView& s, const Uniforms& u, const uint32_t* idx,
-                        const FrameCounters* fc, float4* rec, cudaStream_t st) {
+                        const FrameCounters* fc, float4* rec, uint2* boxes, cudaStream_t st) {
     if (rect)
-        k_preprocess<SHO, COV, true><<<g, 256, 0, st>>>(s, u, idx, fc, rec);
+        k_preprocess<SHO, COV, true><<<g, 256, 0, st>>>(s, u, idx, fc, rec, boxes);
     else
-        k_preprocess<SHO, COV, false><<<g, 256, 0, st>>>(s, u, idx, fc, rec);
+        k_preprocess<SHO, COV, false><<<g, 256, 0, st>>>(s, u, idx, fc, rec, boxes);
 }
 template <int SHO>
 static void launch_pre1(bool cov, bool rect, dim3 g, const SceneView& s, const Uniforms& u, const uint32_t* idx,
-                        const FrameCounters* fc, float4* rec, cudaStream_t st) {
+                        const FrameCounters* fc, float4* rec, uint2* boxes, cudaStream_t st) {
     if (cov)
-        launch_pre2<SHO, true>(rect, g, s, u, idx, fc, rec, st);
+        launch_pre2<SHO, true>(rect, g, s, u, idx, fc, rec, boxes, st);
     else
-        launch_pre2<SHO, false>(rect, g, s, u, idx, fc, rec, st);
+        launch_pre2<SHO, false>(rect, g, s, u, idx, fc, rec, boxes, st);
 }
 
 void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
-                       const uint32_t* idx, const FrameCounters* fc, float4* rec, uint32_t max_n, cudaStream_t st) {
+                       const uint32_t* idx, const FrameCounters* fc, float4* rec, uint2* boxes, uint32_t max_n,
+                       cudaStream_t st) {
     if (max_n == 0) return;
     uint32_t blocks = (max_n + 255) / 256;
     if (blocks > 152u * 16u) blocks = 152u * 16u;
     const dim3 g(blocks);
     switch (sh_order) {
-        case 0: launch_pre1<0>(covariance, rect, g, s, u, idx, fc, rec, st); break;
-        case 1: launch_pre1<1>(covariance, rect, g, s, u, idx, fc, rec, st); break;
-        case 2: launch_pre1<2>(covariance, rect, g, s, u, idx, fc, rec, st); break;
-        default: launch_pre1<3>(covariance, rect, g, s, u, idx, fc, rec, st); break;
+        case 0: launch_pre1<0>(covariance, rect, g, s, u, idx, fc, rec, boxes, st); break;
+        case 1: launch_pre1<1>(covariance, rect, g, s, u, idx, fc, rec, boxes, st); break;
+        case 2: launch_pre1<2>(covariance, rect, g, s, u, idx, fc, rec, boxes, st); break;
+        default: launch_pre1<3>(covariance, rect, g, s, u, idx, fc, rec, boxes, st); break;
     }
 }
 

@@ -17,7 +17,7 @@ namespace spl {
 
 // ------------------------------------------------------------------------------------------------
 template <bool ORDERED>
-__global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order, const float4* __restrict__ rec,
+__global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order, const uint2* __restrict__ boxes,
                                              FrameCounters* fc, int mode, const uint32_t* __restrict__ epoch_word,
                                              uint64_t* status, uint32_t* __restrict__ pair_keys,
                                              uint32_t* __restrict__ pair_vals, uint32_t pair_cap, int tiles_x,
@@ -61,9 +61,8 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
         uint32_t c = 0, slot = 0, box = 0, bw = 0;
         if (r < draw) {
             slot = ORDERED ? __ldg(order + r) : r;
-            const float4 q1 = __ldg(rec + (size_t)slot * 4 + 1);
-            const float4 q2 = __ldg(rec + (size_t)slot * 4 + 2);
-            const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
+            const uint2 bb = __ldg(boxes + slot);
+            const uint32_t lo = bb.x, hi = bb.y;
             const uint32_t x0 = lo & 0xFFFFu, y0 = lo >> 16, x1 = hi & 0xFFFFu, y1 = hi >> 16;
             if (x0 <= x1 && y0 <= y1) {
                 const uint32_t tx0 = x0 / TILE_PIXELS, tx1 = x1 / TILE_PIXELS;
@@ -128,15 +127,15 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
     }
 }
 
-void launch_bin(int mode, const uint32_t* order, const float4* rec, FrameCounters* fc, const uint32_t* epoch_word,
+void launch_bin(int mode, const uint32_t* order, const uint2* boxes, FrameCounters* fc, const uint32_t* epoch_word,
                 uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals, uint32_t pair_cap, int tiles_x,
                 uint32_t max_n, uint32_t spin_limit, cudaStream_t st) {
     const uint32_t grid = max_n == 0 ? 1u : (max_n + BIN_TILE - 1) / BIN_TILE;
     if (order)
-        k_bin<true><<<grid, 256, 0, st>>>(order, rec, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
+        k_bin<true><<<grid, 256, 0, st>>>(order, boxes, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
                                           tiles_x, spin_limit);
     else
-        k_bin<false><<<grid, 256, 0, st>>>(order, rec, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
+        k_bin<false><<<grid, 256, 0, st>>>(order, boxes, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
                                            tiles_x, spin_limit);
 }
 
@@ -162,13 +161,17 @@ void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint
 // ------------------------------------------------------------------------------------------------
 constexpr int RASTER_BATCH = 256;
 
-// One CTA per 16x16 tile, one thread per pixel; warp w owns the 16x2 strip of rows 2w, 2w+1.  The
-// tile's records (depth order) are staged through shared memory in batches of 256.  For each batch a
-// warp first builds its relevance list with ballots (32 box tests per instruction slot, in order),
-// then evaluates only the records whose pixel box meets its strip.  Per pixel: box test, coverage
-// test, falloff, 1/255 discard, blend — the same operations as the oracle's raster_tile, so the
-// image is bit-identical.  A warp whose pixels are all finished skips the rest of the list, and the
-// CTA stops once every pixel is finished (T == 0 in unorm8 mode, T < 1e-4 in fp32 mode).
+// One CTA per 16x16 tile, one thread per pixel.  Warp w owns rows 2w, 2w+1, split into four 4x2-pixel
+// groups of 8 lanes (group g = lane / 8 covers columns 4g..4g+3).  The tile's records (depth order)
+// are staged through shared memory in batches of 256.  For each chunk of 32 records a lane tests one
+// record's pixel box against the four groups' blocks; four ballots give each group its relevance
+// list, in order.  The warp then walks the four lists at once: in every iteration each group takes
+// its next record, so one pass of the per-pixel code serves up to four splats (most splats here
+// cover a few pixels, so this keeps far more lanes busy than a whole warp per splat).  Per pixel:
+// box test, coverage test, falloff, 1/255 discard, blend — the operations of the oracle's
+// raster_tile in the same order, so the image is bit-identical.  Lists are walked in depth order per
+// pixel, a warp whose pixels are all finished skips the rest, and the CTA stops once every pixel is
+// finished (T == 0 in unorm8 mode, T < 1e-4 in fp32 mode).
 template <bool RECT, int BLEND>
 __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ pair_vals,
                                                 const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
@@ -176,21 +179,23 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     __shared__ float4 s_q0[RASTER_BATCH], s_q1[RASTER_BATCH], s_q2[RASTER_BATCH];
     __shared__ float4 s_q3[RECT ? 1 : RASTER_BATCH];
     __shared__ float s_lut[256];
-    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
+    const uint32_t grp = lane >> 3, li = lane & 7u;
     const int tile = blockIdx.x;
     const int tx = tile % tiles_x, ty = tile / tiles_x;
-    const int px = tx * TILE_PIXELS + (int)(tid & 15u), py = ty * TILE_PIXELS + (int)(tid >> 4);
+    const int bx0 = tx * TILE_PIXELS + 4 * (int)grp;  // this lane's 4x2 block
+    const int by0 = ty * TILE_PIXELS + 2 * (int)w;
+    const int px = bx0 + (int)(li & 3u), py = by0 + (int)(li >> 2);
     const float X = (float)px + 0.5f, Y = (float)py + 0.5f;
     s_lut[tid] = (float)tid / 255.0f;
     const uint2 rg = ranges[tile];
-    const int wy0 = ty * TILE_PIXELS + (int)(tid >> 5) * 2, wy1 = wy0 + 1;
-    const int wx0 = tx * TILE_PIXELS, wx1 = wx0 + TILE_PIXELS - 1;
     const bool inside = px < W && py < H;
     bool done = !inside;
     bool warp_done = __all_sync(FULL_MASK, done);
     int cr = 0, cg = 0, cb = 0, ta = 255;
     float fr = 0.0f, fg = 0.0f, fb = 0.0f, ft = 1.0f;
     const float alpha_min = 1.0f / 255.0f;
+    const int wx0 = tx * TILE_PIXELS;  // the four blocks of this warp: columns wx0 + 4g .. + 3, rows by0, by0+1
     for (uint32_t b = rg.x; b < rg.y; b += RASTER_BATCH) {
         __syncthreads();
         const uint32_t i = b + tid;
@@ -206,17 +211,29 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
         const uint32_t cnt = min((uint32_t)RASTER_BATCH, rg.y - b);
         if (!warp_done) {
             for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
-                bool rel = false;
-                const uint32_t jl = j0 + lane;
-                if (jl < cnt) {
-                    const uint32_t lo = __float_as_uint(s_q1[jl].w), hi = __float_as_uint(s_q2[jl].w);
-                    rel = !((int)(hi & 0xFFFFu) < wx0 || (int)(lo & 0xFFFFu) > wx1 || (int)(hi >> 16) < wy0 ||
-                            (int)(lo >> 16) > wy1);
+                // relevance of record j0 + lane for each of the warp's four blocks
+                uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+                {
+                    const uint32_t jl = j0 + lane;
+                    int x0 = 1, x1 = 0, y0 = 1, y1 = 0;
+                    if (jl < cnt) {
+                        const uint32_t lo = __float_as_uint(s_q1[jl].w), hi = __float_as_uint(s_q2[jl].w);
+                        x0 = (int)(lo & 0xFFFFu);
+                        y0 = (int)(lo >> 16);
+                        x1 = (int)(hi & 0xFFFFu);
+                        y1 = (int)(hi >> 16);
+                    }
+                    const bool rows = !(y1 < by0 || y0 > by0 + 1) && x0 <= x1;
+                    m0 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 0 || x0 > wx0 + 3));
+                    m1 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 4 || x0 > wx0 + 7));
+                    m2 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 8 || x0 > wx0 + 11));
+                    m3 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 12 || x0 > wx0 + 15));
                 }
-                uint32_t mask = __ballot_sync(FULL_MASK, rel);
-                while (mask) {
-                    const uint32_t j = j0 + (uint32_t)(__ffs(mask) - 1);
-                    mask &= mask - 1u;
+                uint32_t mine = grp == 0 ? m0 : (grp == 1 ? m1 : (grp == 2 ? m2 : m3));
+                while (__any_sync(FULL_MASK, mine != 0u)) {
+                    if (mine == 0u) continue;
+                    const uint32_t j = j0 + (uint32_t)(__ffs(mine) - 1);
+                    mine &= mine - 1u;
                     const float4 q1 = s_q1[j], q2 = s_q2[j];
                     const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
                     const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);

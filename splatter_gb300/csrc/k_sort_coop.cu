@@ -3,39 +3,53 @@
 // The reference's GPU depth sort (radixSortA/B/C, Lichtso/splatter src/shaders.wgsl:298-498) is a
 // onesweep sort whose tiles learn their global digit offsets through a decoupled look-back chain.
 // At splat-pipeline sizes (a few million keys, L2-resident) that chain — one L2 round trip per
-// tile — dominates.  Here every CTA is resident (cooperative launch, one 1024-thread CTA per SM) and
+// tile — dominates.  Here every CTA is resident (cooperative launch, two 512-thread CTAs per SM) and
 // owns one contiguous segment of the input; each 8-bit pass is:
 //   1. count: the segment's digit histogram -> cnt[digit][cta]                       (global)
-//   2. bounded grid barrier
-//   3. offsets: for each digit, the exclusive prefix over earlier CTAs plus the global digit base,
-//      from one sweep over cnt[digit][*] (vector loads)
-//   4. scatter, sub-tile by sub-tile (8192 keys): warp-level multisplit ranking (__match_any_sync),
+//   2. bounded grid barrier; CTA d scans digit row d in place (exclusive prefix over CTAs) and
+//      writes the row total; bounded grid barrier
+//   3. offsets: each CTA reads its column of prefixes and the 256 totals (global digit bases)
+//   4. scatter, sub-tile by sub-tile (4096 keys): warp-level multisplit ranking (digit match by eight
+//      ballots),
 //      per-digit warp prefixes, keys then values staged through shared memory and written as runs
 //   5. bounded grid barrier (the next pass reads this pass's output)
 // The ranking keeps equal digits in input order, so every pass is stable, like the onesweep passes.
 // Every barrier wait is bounded: on timeout the error bit is raised and the kernel runs to its end
 // (writes stay in bounds), so a missing CTA can never hang the GPU.
-#include <cooperative_groups.h>
-
 #include "spl_device.cuh"
 
 namespace spl {
 
-constexpr int CS_THREADS = 1024;
+constexpr int CS_THREADS = 512;               // two CTAs per SM
 constexpr int CS_WARPS = CS_THREADS / 32;
+constexpr int CS_NQ = CS_THREADS / 256;        // threads per digit in the per-digit phases
+constexpr int CS_WPQ = CS_WARPS / CS_NQ;       // warps summed by one of those threads
 constexpr int CS_KPT = 8;
-constexpr int CS_TILE = CS_THREADS * CS_KPT;  // 8192 keys per sub-tile
+constexpr int CS_TILE = CS_THREADS * CS_KPT;  // 4096 keys per sub-tile
 
 struct CoopSmem {
-    uint32_t buf[CS_TILE];             // 32 KB staging for keys, then values
-    uint32_t wcnt[CS_WARPS][256];      // per-warp digit counts -> exclusive prefixes (32 KB)
-    uint32_t part[4][256];             // partial sums of 8 warps each / of CTA quarters
+    uint32_t buf[CS_TILE];             // staging for keys, then values
+    uint32_t wcnt[CS_WARPS][256];      // per-warp digit counts -> exclusive prefixes
+    uint32_t part[CS_NQ][256];         // partial sums over groups of warps / of the count table
     uint32_t base[256];                // global output base of each digit for this CTA
     uint32_t running[256];             // keys of each digit already written by this CTA
     uint32_t dstart[256];              // tile-local exclusive digit offsets
     uint32_t tcount[256];              // tile digit counts
-    uint32_t scan[32];
+    uint32_t scan[CS_WARPS];
 };
+
+// Lanes whose 8-bit digit equals this lane's (valid lanes only), from eight ballots: the warp-level
+// multisplit match without MATCH.ANY, whose latency dominated the ranking.
+__device__ __forceinline__ uint32_t match_digit(uint32_t d, bool valid) {
+    uint32_t peers = __ballot_sync(FULL_MASK, valid);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t m = __ballot_sync(FULL_MASK, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
 
 __device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t spin_limit, uint32_t* err) {
     __syncthreads();
@@ -64,7 +78,7 @@ __device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t nblocks, ui
 }
 
 // Block-wide exclusive scan over 256 values held by threads 0..255 (other threads pass 0 and ignore
-// the result).  Uses sm->scan; all 1024 threads must call it.
+// the result).  Uses sm->scan; every thread of the CTA must call it.
 __device__ __forceinline__ uint32_t scan256(uint32_t v, uint32_t* scan, uint32_t* total) {
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     uint32_t x = v;
@@ -90,14 +104,17 @@ __device__ __forceinline__ uint32_t scan256(uint32_t v, uint32_t* scan, uint32_t
 // keys0 -> keys1 -> keys0 ... for `passes` passes starting at bit `shift0`; vals likewise (both value
 // buffers are real; with iota_first the values read by pass 0 are the input positions instead of
 // vals0).  The result of pass p is in keys1/vals1 for even p and keys0/vals0 for odd p.
-__global__ void __launch_bounds__(CS_THREADS, 1)
+__global__ void __launch_bounds__(CS_THREADS, 2)
     k_sort_coop(uint32_t* keys0, uint32_t* keys1, uint32_t* vals0, uint32_t* vals1, int iota_first,
-                const uint32_t* n_ptr, uint32_t n_cap, int passes, int shift0, uint32_t* cnt /*[256][gridDim]*/,
+                const uint32_t* n_ptr, uint32_t n_cap, int passes, int shift0, uint32_t* cnt /*[256][Gp] + tot[256]*/,
                 uint32_t* bar, uint32_t spin_limit, uint32_t* err) {
+    // cnt rows: [256][Gp], Gp = gridDim rounded up to a multiple of 4 so rows are 16-byte aligned
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CoopSmem& sm = *reinterpret_cast<CoopSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     const uint32_t G = gridDim.x, c = blockIdx.x;
+    const uint32_t Gp = (G + 3u) & ~3u;  // padded row stride of cnt (16-byte rows)
+    uint32_t* tot = cnt + (size_t)256 * Gp;  // per-digit totals of a pass
     const uint32_t n = min(*n_ptr, n_cap);
     // contiguous segments, 256-aligned
     uint32_t seg = (n + G - 1) / G;
@@ -111,65 +128,120 @@ __global__ void __launch_bounds__(CS_THREADS, 1)
         uint32_t* kout = (p & 1) ? keys0 : keys1;
         uint32_t* vout = (p & 1) ? vals0 : vals1;
         const bool iota = (p == 0 && iota_first != 0);
-        // ---- 1. count ----
-        if (tid < 256) sm.part[0][tid] = 0u;
+        // ---- 1. count: per-warp histograms (shared atomics) ----
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sm.wcnt[w][lane + 32 * k] = 0u;
+        __syncwarp();
+        {
+            // 16-byte loads (segments start 256-aligned), four in flight per thread; the loads bypass
+            // L1 because the previous pass's output was written by other CTAs of this launch
+            // s_begin is a multiple of 256 unless the segment is empty (s_begin == s_end == n)
+            const uint32_t v_begin = s_begin >> 2, v_end = max(v_begin, s_end >> 2);
+            const uint4* kin4 = reinterpret_cast<const uint4*>(kin);
+            for (uint32_t v0 = v_begin; v0 < v_end; v0 += 4u * CS_THREADS) {
+                uint4 q[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t vi = v0 + (uint32_t)u * CS_THREADS + tid;
+                    q[u] = vi < v_end ? __ldcg(kin4 + vi) : make_uint4(0u, 0u, 0u, 0u);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (v0 + (uint32_t)u * CS_THREADS + tid < v_end) {
+                        atomicAdd(&sm.wcnt[w][(q[u].x >> shift) & 255u], 1u);
+                        atomicAdd(&sm.wcnt[w][(q[u].y >> shift) & 255u], 1u);
+                        atomicAdd(&sm.wcnt[w][(q[u].z >> shift) & 255u], 1u);
+                        atomicAdd(&sm.wcnt[w][(q[u].w >> shift) & 255u], 1u);
+                    }
+                }
+            }
+            // tail (fewer than 4 keys past the last 16-byte group)
+            for (uint32_t e = max(v_end << 2, s_begin) + tid; e < s_end; e += CS_THREADS)
+                atomicAdd(&sm.wcnt[w][(__ldcg(kin + e) >> shift) & 255u], 1u);
+        }
         __syncthreads();
-        // (loads bypass L1: the previous pass's output was written by other CTAs of this launch)
-        for (uint32_t e = s_begin + tid; e < s_end; e += CS_THREADS)
-            atomicAdd(&sm.part[0][(__ldcg(kin + e) >> shift) & 255u], 1u);
-        __syncthreads();
-        if (tid < 256) cnt[(size_t)tid * G + c] = sm.part[0][tid];
-        grid_barrier(bar, G, spin_limit, err);
-        // ---- 3. offsets: thread (d = tid & 255, q = tid >> 8) sweeps a quarter of cnt[d][*] ----
         {
             const uint32_t d = tid & 255u, q = tid >> 8;
-            const uint32_t per = (G + 3u) / 4u;
-            const uint32_t cb = q * per, ce = min(cb + per, G);
-            uint32_t pre = 0, tot = 0;
-            const uint32_t* row = cnt + (size_t)d * G;
-            for (uint32_t k = cb; k < ce; ++k) {
-                const uint32_t v = __ldcg(row + k);
-                tot += v;
-                pre += k < c ? v : 0u;
-            }
-            sm.part[q][d] = tot;
-            sm.wcnt[q][d] = pre;  // wcnt is free here; borrow 4 rows
-        }
-        __syncthreads();
-        uint32_t dtotal = 0, dpre = 0;
-        if (tid < 256) {
+            uint32_t acc = 0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                dtotal += sm.part[q][tid];
-                dpre += sm.wcnt[q][tid];
-            }
-        }
-        uint32_t all;
-        const uint32_t gdig = scan256(tid < 256 ? dtotal : 0u, sm.scan, &all);
-        if (tid < 256) {
-            sm.base[tid] = gdig + dpre;
-            sm.running[tid] = 0u;
+            for (int k = 0; k < CS_WPQ; ++k) acc += sm.wcnt[CS_WPQ * q + k][d];
+            sm.part[q][d] = acc;
         }
         __syncthreads();
+        if (tid < 256) {
+            uint32_t acc = 0;
+#pragma unroll
+            for (int q = 0; q < CS_NQ; ++q) acc += sm.part[q][tid];
+            cnt[(size_t)tid * Gp + c] = acc;
+        }
+        __syncthreads();
+        grid_barrier(bar, G, spin_limit, err);
+        // ---- 3a. distributed scan: CTA c turns the digit rows d = c, c + G, ... of cnt[d][0..G) into
+        //          their exclusive prefixes over CTAs and writes the row totals to tot[d] ----
+        for (uint32_t d = c; d < 256u; d += G) {  // uniform across the CTA
+            uint32_t* row = cnt + (size_t)d * Gp;
+            uint32_t carry = 0;
+            for (uint32_t k0 = 0; k0 < G; k0 += CS_THREADS) {  // uniform across the CTA
+                const uint32_t k = k0 + tid;
+                const uint32_t v = k < G ? __ldcg(row + k) : 0u;
+                uint32_t x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
+                    if (lane >= (uint32_t)o) x += y;
+                }
+                if (lane == 31) sm.scan[w] = x;
+                __syncthreads();
+                uint32_t wpre = 0, ctot = 0;
+#pragma unroll
+                for (uint32_t i = 0; i < (uint32_t)CS_WARPS; ++i) {
+                    const uint32_t t = sm.scan[i];
+                    wpre += i < w ? t : 0u;
+                    ctot += t;
+                }
+                __syncthreads();
+                if (k < G) row[k] = carry + wpre + x - v;
+                carry += ctot;
+            }
+            if (tid == 0) tot[d] = carry;
+        }
+        grid_barrier(bar, G, spin_limit, err);
+        // ---- 3b. offsets: this CTA's column of prefixes plus the global digit bases ----
+        {
+            uint32_t dtotal = 0, dpre = 0;
+            if (tid < 256) {
+                dpre = __ldcg(cnt + (size_t)tid * Gp + c);
+                dtotal = __ldcg(tot + tid);
+            }
+            uint32_t all;
+            const uint32_t gdig = scan256(tid < 256 ? dtotal : 0u, sm.scan, &all);
+            if (tid < 256) {
+                sm.base[tid] = gdig + dpre;
+                sm.running[tid] = 0u;
+            }
+            __syncthreads();
+        }
         // ---- 4. scatter, sub-tile by sub-tile ----
         for (uint32_t tb = s_begin; tb < s_end; tb += CS_TILE) {
             const uint32_t tn = min((uint32_t)CS_TILE, s_end - tb);
 #pragma unroll
             for (int k = 0; k < 8; ++k) sm.wcnt[w][lane + 32 * k] = 0u;
             __syncwarp();
-            uint32_t key[CS_KPT], pos[CS_KPT];
+            uint32_t key[CS_KPT], pos[CS_KPT], val[CS_KPT];
             const uint32_t wb = tb + w * 256u + lane;
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
                 const uint32_t e = wb + 32u * j;
-                key[j] = e < tb + tn ? __ldcg(kin + e) : 0u;
+                const bool ok = e < tb + tn;
+                key[j] = ok ? __ldcg(kin + e) : 0u;
+                val[j] = ok ? (iota ? e : __ldcg(vin + e)) : 0u;
             }
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
                 const uint32_t e = wb + 32u * j;
                 const bool valid = e < tb + tn;
-                const uint32_t d = valid ? (key[j] >> shift) & 255u : 256u;
-                const uint32_t peers = __match_any_sync(FULL_MASK, d);
+                const uint32_t d = (key[j] >> shift) & 255u;
+                const uint32_t peers = match_digit(d, valid);
                 uint32_t cur = 0;
                 if (valid) cur = sm.wcnt[w][d];
                 __syncwarp();
@@ -178,14 +250,14 @@ __global__ void __launch_bounds__(CS_THREADS, 1)
                 pos[j] = cur + __popc(peers & lt);
             }
             __syncthreads();
-            // per digit: exclusive prefix over the 32 warps (thread (d, q) handles warps 8q..8q+7)
+            // per digit: exclusive prefix over the warps (thread (d, q) handles warps CS_WPQ*q ..)
             {
                 const uint32_t d = tid & 255u, q = tid >> 8;
                 uint32_t s = 0;
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const uint32_t v = sm.wcnt[8 * q + k][d];
-                    sm.wcnt[8 * q + k][d] = s;
+                for (int k = 0; k < CS_WPQ; ++k) {
+                    const uint32_t v = sm.wcnt[CS_WPQ * q + k][d];
+                    sm.wcnt[CS_WPQ * q + k][d] = s;
                     s += v;
                 }
                 sm.part[q][d] = s;
@@ -195,13 +267,17 @@ __global__ void __launch_bounds__(CS_THREADS, 1)
                 const uint32_t d = tid & 255u, q = tid >> 8;
                 uint32_t add = 0;
 #pragma unroll
-                for (uint32_t k = 0; k < 4; ++k) add += k < q ? sm.part[k][d] : 0u;
+                for (uint32_t k = 0; k < (uint32_t)CS_NQ; ++k) add += k < q ? sm.part[k][d] : 0u;
                 if (add) {
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) sm.wcnt[8 * q + k][d] += add;
+                    for (int k = 0; k < CS_WPQ; ++k) sm.wcnt[CS_WPQ * q + k][d] += add;
                 }
             }
-            const uint32_t tc = tid < 256 ? ((sm.part[0][tid] + sm.part[1][tid]) + (sm.part[2][tid] + sm.part[3][tid])) : 0u;
+            uint32_t tc = 0;
+            if (tid < 256) {
+#pragma unroll
+                for (int q = 0; q < CS_NQ; ++q) tc += sm.part[q][tid];
+            }
             uint32_t tt;
             const uint32_t ds = scan256(tc, sm.scan, &tt);  // contains __syncthreads
             if (tid < 256) {
@@ -235,7 +311,7 @@ __global__ void __launch_bounds__(CS_THREADS, 1)
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
                 const uint32_t e = wb + 32u * j;
-                if (e < tb + tn) sm.buf[pos[j]] = iota ? e : __ldcg(vin + e);
+                if (e < tb + tn) sm.buf[pos[j]] = val[j];
             }
             __syncthreads();
 #pragma unroll

@@ -72,14 +72,15 @@ void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st
 void launch_cull_key(int mode, const SceneView& s, const Uniforms& u, FrameCounters* fc, const uint32_t* epoch_word,
                      uint64_t* status, uint32_t* keys_out, uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st);
 void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
-                       const uint32_t* idx, const FrameCounters* fc, float4* rec, uint32_t max_n, cudaStream_t st);
+                       const uint32_t* idx, const FrameCounters* fc, float4* rec, uint2* boxes, uint32_t max_n,
+                       cudaStream_t st);
 // One LSD onesweep pass over 8 bits at `shift`.  n = min(*n_ptr, n_cap).  vals_in == nullptr means
 // values are the input positions (0, 1, 2, ...).
 void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                      const uint32_t* n_ptr, uint32_t n_cap, const uint32_t* hist256, uint64_t* status,
                      uint32_t* tile_counter, const uint32_t* epoch_word, int shift, uint32_t spin_limit,
                      uint32_t* err, cudaStream_t st);
-void launch_bin(int mode, const uint32_t* order, const float4* rec, FrameCounters* fc, const uint32_t* epoch_word,
+void launch_bin(int mode, const uint32_t* order, const uint2* boxes, FrameCounters* fc, const uint32_t* epoch_word,
                 uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals, uint32_t pair_cap, int tiles_x,
                 uint32_t max_n, uint32_t spin_limit, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint32_t pair_cap, uint2* ranges,

@@ -165,6 +165,30 @@ SPL_API int spl_scene_write_splats(spl_scene* s, const float* splats60, uint64_t
 /* Reads splats back in the same 60-float layout into host memory (synchronous). */
 SPL_API int spl_scene_read_splats(const spl_scene* s, float* splats60, uint64_t start, uint64_t count);
 
+/* A scene over caller-owned device arrays (no copy; the arrays must outlive the scene and are not
+ * freed by spl_scene_destroy): planes x[n], y[n], z[n]; rotation[n][4] (scalar first, used as given —
+ * the file loader normalises, scene.rs:227); scale_alpha[n][4] (scale xyz, opacity); sh[n][48].  The
+ * last three must be 16-byte aligned.  This is how a training loop renders parameters it owns. */
+SPL_API int spl_scene_wrap(spl_renderer* r, uint64_t splat_count, float* x, float* y, float* z, float* rotation,
+                           float* scale_alpha, float* sh, spl_scene** out);
+
+/* ---- backward pass (no reference counterpart) ------------------------------------------------------- */
+/* Gradients of the renderer's LAST frame of `scene` (rendered with blend_mode SPL_BLEND_FP32) with
+ * respect to the splat parameters, given the frame's float4 image (r, g, b, T) and dL/d(image)
+ * (float4 per pixel).  Writes, for every splat that was drawn, grad_x/y/z[i], grad_rotation[i][4],
+ * grad_scale_alpha[i][4] (scale xyz, opacity) and grad_sh[i][48]; splats that were not drawn are left
+ * untouched (zero the arrays first).  Transmittance is recomputed per tile, not stored; depth order,
+ * culling and the 1/255 discard are treated as constants.  Asynchronous on `stream`. */
+SPL_API int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
+                                const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z,
+                                float* grad_rotation, float* grad_scale_alpha, float* grad_sh, void* stream);
+
+/* Copies the last backward pass's per-record gradients (10 floats per visible splat, compaction
+ * order: d/dA00, d/dA01, d/dB0, d/dA10, d/dA11, d/dB1 with A taken against pixel offsets from the
+ * centre of the record's pixel box and B at that centre, then d/dopacity, d/dr, d/dg, d/db) into a
+ * device array of `capacity` records.  Diagnostics.  Asynchronous on `stream`. */
+SPL_API int spl_renderer_copy_record_gradients(spl_renderer* r, float* dst_device, uint64_t capacity, void* stream);
+
 /* ---- device sort (radixSortB/radixSortC, shaders.wgsl:338-498) --------------------------------- */
 /* Stable LSD onesweep sort of `count` (key, value) pairs on the device: keys_in/values_in are
  * sorted into keys_out/values_out by the low `key_bits` bits of the key (8, 16, 24 or 32).

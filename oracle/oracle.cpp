@@ -99,6 +99,44 @@ struct Num<double> {
     static constexpr double SQRT2 = 1.41421356237309504880;
 };
 
+// Forward-mode dual number in FP64 (value, derivative): the FP64 reference gradient of the vertex
+// stage runs the same template on it, once per input direction.
+struct Dd {
+    double v, d;
+    Dd(double x = 0.0) : v(x), d(0.0) {}
+    Dd(double x, double dx) : v(x), d(dx) {}
+};
+inline Dd operator+(Dd a, Dd b) { return {a.v + b.v, a.d + b.d}; }
+inline Dd operator-(Dd a, Dd b) { return {a.v - b.v, a.d - b.d}; }
+inline Dd operator*(Dd a, Dd b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dd operator/(Dd a, Dd b) {
+    const double q = a.v / b.v;
+    return {q, (a.d - q * b.d) / b.v};
+}
+inline Dd operator-(Dd a) { return {-a.v, -a.d}; }
+inline bool operator<(Dd a, Dd b) { return a.v < b.v; }
+inline bool operator>(Dd a, Dd b) { return a.v > b.v; }
+template <>
+struct Num<Dd> {
+    static Dd sqrt(Dd x) {
+        const double r = std::sqrt(x.v);
+        return {r, r > 0.0 ? x.d / (2.0 * r) : 0.0};
+    }
+    static constexpr double SQRT2 = 1.41421356237309504880;
+};
+inline float o_min(float a, float b) { return std::fmin(a, b); }
+inline float o_max(float a, float b) { return std::fmax(a, b); }
+inline double o_min(double a, double b) { return std::fmin(a, b); }
+inline double o_max(double a, double b) { return std::fmax(a, b); }
+inline Dd o_min(Dd a, Dd b) { return std::fmin(a.v, b.v) == a.v ? a : b; }
+inline Dd o_max(Dd a, Dd b) { return std::fmax(a.v, b.v) == a.v ? a : b; }
+inline float o_abs(float a) { return std::fabs(a); }
+inline double o_abs(double a) { return std::fabs(a); }
+inline Dd o_abs(Dd a) { return a.v < 0.0 ? -a : a; }
+inline double o_val(float a) { return a; }
+inline double o_val(double a) { return a; }
+inline double o_val(Dd a) { return a.v; }
+
 // Uniform block, byte-compatible with `Uniforms` (renderer.rs:49-61; shaders.wgsl:1-11).
 struct OU {
     float camera[16];  // column-major, camera-to-world
@@ -201,8 +239,8 @@ void projected_covariance(const OU& u, const F* s, const F* rot, const F* t, F* 
     for (int r = 0; r < 3; ++r)
         v[r] = (((F)u.view[0 * 4 + r] * t[0] + (F)u.view[1 * 4 + r] * t[1]) + (F)u.view[2 * 4 + r] * t[2]) +
                (F)u.view[3 * 4 + r] * F(1);
-    v[0] = std::fmin(std::fmax(v[0] / v[2], F(-1)), F(1)) * v[2];
-    v[1] = std::fmin(std::fmax(v[1] / v[2], F(-1)), F(1)) * v[2];
+    v[0] = o_min(o_max(v[0] / v[2], F(-1)), F(1)) * v[2];
+    v[1] = o_min(o_max(v[1] / v[2], F(-1)), F(1)) * v[2];
     const F zz = v[2] * v[2];
     const F J[9] = {F(1) / v[2], F(0), (-v[0]) / zz, F(0), F(1) / v[2], (-v[1]) / zz, F(0), F(0), F(0)};
     F Tt[9], TC[9], Tm[9], Tmt[9];
@@ -256,8 +294,8 @@ void ellipse_scale(const F* M, const F* t, const F* r, F* out) {
     const F xx = M[0], xy = M[1], yy = M[4], zz = M[8];
     const F d = ((F(2) * xy) * r[0]) * r[1];
     const F e = zz - (((xx * t[0]) * t[0] + (yy * t[1]) * t[1]) + ((F(2) * xy) * t[0]) * t[1]);
-    out[0] = Num<F>::sqrt(std::fabs(e / (((xx * r[1]) * r[1] + (yy * r[0]) * r[0]) - d)));
-    out[1] = Num<F>::sqrt(std::fabs(e / (((xx * r[0]) * r[0] + (yy * r[1]) * r[1]) + d)));
+    out[0] = Num<F>::sqrt(o_abs(e / (((xx * r[1]) * r[1] + (yy * r[0]) * r[0]) - d)));
+    out[1] = Num<F>::sqrt(o_abs(e / (((xx * r[0]) * r[0] + (yy * r[1]) * r[1]) + d)));
 }
 
 // extractScaleOfCovariance (shaders.wgsl:240-246).
@@ -290,6 +328,8 @@ template <>
 inline float shc<float>(int i) { return SHC_F[i]; }
 template <>
 inline double shc<double>(int i) { return SHC_D[i]; }
+template <>
+inline Dd shc<Dd>(int i) { return Dd(SHC_D[i]); }
 
 template <typename F>
 void sh_lookup(const F* d, const F* sh, int order, F* rgb) {
@@ -336,23 +376,27 @@ struct Dbg {
     F t[2], r[2], axes[2], rgb[3];
 };
 
+// What the vertex stage derives from one splat (the quantities the raster and the gradients use).
 template <typename F>
-bool preprocess_one(const OU& u, const OCfg& cfg, const float* center, const float* rot, const float* scale,
-                    float alpha, const float* sh, float* rec, Dbg<F>* dbg) {
-    F c[3] = {(F)center[0], (F)center[1], (F)center[2]};
-    F q[4] = {(F)rot[0], (F)rot[1], (F)rot[2], (F)rot[3]};
+struct VOut {
+    F A00, A01, B0, A10, A11, B1;  // tc = A (X, Y) + B at the pixel centre (X, Y)
+    F rgb[3];
+    F Xx, Xy, Yx, Yy, Zx, Zy;      // rect basis and centre in view-plane units
+    F bx, by;                      // AA-square offsets
+    Dbg<F> dbg;
+};
+
+// The vertex stage (shaders.wgsl:507-573) restated; scale is the splat's scale before splat_scale.
+template <typename F>
+void vertex_core(const OU& u, const OCfg& cfg, const F* c, const F* q, const F* scale, const F* shf, VOut<F>& o) {
     F se[3];
-    for (int i = 0; i < 3; ++i) se[i] = (F)scale[i] * (F)u.splat_scale;
-    F shf[48];
-    const int nsh = 3 * (cfg.sh_order + 1) * (cfg.sh_order + 1);
-    for (int i = 0; i < nsh; ++i) shf[i] = (F)sh[i];
+    for (int i = 0; i < 3; ++i) se[i] = scale[i] * (F)u.splat_scale;
     // colour (shaders.wgsl:531-532)
     F v[3];
     for (int i = 0; i < 3; ++i) v[i] = c[i] - (F)u.camera[12 + i];
     const F len = Num<F>::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
     F d[3] = {v[0] / len, v[1] / len, v[2] / len};
-    F rgb[3];
-    sh_lookup(d, shf, cfg.sh_order, rgb);
+    sh_lookup(d, shf, cfg.sh_order, o.rgb);
     // conic and its decomposition (shaders.wgsl:533-542)
     F M[9], t[2], r[2], axes[2];
     projected_contour(u, se, q, c, M);
@@ -365,29 +409,48 @@ bool preprocess_one(const OU& u, const OCfg& cfg, const float* center, const flo
     } else {
         ellipse_scale(M, t, r, axes);
     }
-    if (dbg) {
-        for (int i = 0; i < 9; ++i) dbg->M[i] = M[i];
-        dbg->t[0] = t[0]; dbg->t[1] = t[1];
-        dbg->r[0] = r[0]; dbg->r[1] = r[1];
-        dbg->axes[0] = axes[0]; dbg->axes[1] = axes[1];
-        for (int i = 0; i < 3; ++i) dbg->rgb[i] = rgb[i];
-    }
+    for (int i = 0; i < 9; ++i) o.dbg.M[i] = M[i];
+    o.dbg.t[0] = t[0]; o.dbg.t[1] = t[1];
+    o.dbg.r[0] = r[0]; o.dbg.r[1] = r[1];
+    o.dbg.axes[0] = axes[0]; o.dbg.axes[1] = axes[1];
+    for (int i = 0; i < 3; ++i) o.dbg.rgb[i] = o.rgb[i];
     // rect basis (shaders.wgsl:543-547)
     const F bias = (F)u.bias;
     const F sa = bias + axes[0], sb = bias + axes[1];
-    const F Xx = r[1] * sa, Xy = (-r[0]) * sa;
-    const F Yx = r[0] * sb, Yy = r[1] * sb;
-    const F Zx = t[0], Zy = t[1];
+    o.Xx = r[1] * sa; o.Xy = (-r[0]) * sa;
+    o.Yx = r[0] * sb; o.Yy = r[1] * sb;
+    o.Zx = t[0]; o.Zy = t[1];
     // inverse of the 2x2 basis (shaders.wgsl:563-566), folded with pixel -> view-plane mapping
-    const F det = Xx * Yy - Xy * Yx;
+    const F det = o.Xx * o.Yy - o.Xy * o.Yx;
     const F idet = F(1) / det;
-    const F i00 = Yy * idet, i01 = (-Yx) * idet, i10 = (-Xy) * idet, i11 = Xx * idet;
+    const F i00 = o.Yy * idet, i01 = (-o.Yx) * idet, i10 = (-o.Xy) * idet, i11 = o.Xx * idet;
     const F vw = (F)u.view_size[0], vh = (F)u.view_size[1];
     const F Wf = (F)u.image_size[0], Hf = (F)u.image_size[1];
     const F sx = (F(2) * vw) / Wf, sy = -((F(2) * vh) / Hf);
-    const F bx = (-vw) - Zx, by = vh - Zy;
-    const F A00 = i00 * sx, A01 = i01 * sy, B0 = i00 * bx + i01 * by;
-    const F A10 = i10 * sx, A11 = i11 * sy, B1 = i10 * bx + i11 * by;
+    o.bx = (-vw) - o.Zx;
+    o.by = vh - o.Zy;
+    o.A00 = i00 * sx; o.A01 = i01 * sy; o.B0 = i00 * o.bx + i01 * o.by;
+    o.A10 = i10 * sx; o.A11 = i11 * sy; o.B1 = i10 * o.bx + i11 * o.by;
+}
+
+template <typename F>
+bool preprocess_one(const OU& u, const OCfg& cfg, const float* center, const float* rot, const float* scale,
+                    float alpha, const float* sh, float* rec, Dbg<F>* dbg) {
+    F c[3] = {(F)center[0], (F)center[1], (F)center[2]};
+    F q[4] = {(F)rot[0], (F)rot[1], (F)rot[2], (F)rot[3]};
+    F sc[3] = {(F)scale[0], (F)scale[1], (F)scale[2]};
+    F shf[48];
+    const int nsh = 3 * (cfg.sh_order + 1) * (cfg.sh_order + 1);
+    for (int i = 0; i < nsh; ++i) shf[i] = (F)sh[i];
+    VOut<F> o;
+    vertex_core(u, cfg, c, q, sc, shf, o);
+    if (dbg) *dbg = o.dbg;
+    const F Xx = o.Xx, Xy = o.Xy, Yx = o.Yx, Yy = o.Yy, Zx = o.Zx, Zy = o.Zy;
+    const F A00 = o.A00, A01 = o.A01, B0 = o.B0, A10 = o.A10, A11 = o.A11, B1 = o.B1, bx = o.bx, by = o.by;
+    const F* rgb = o.rgb;
+    const F vw = (F)u.view_size[0], vh = (F)u.view_size[1];
+    const F Wf = (F)u.image_size[0], Hf = (F)u.image_size[1];
+    const F sx = (F(2) * vw) / Wf, sy = -((F(2) * vh) / Hf);
     const F m = (F)u.margin;
     F ex, ey, R = F(0);
     if (cfg.use_unaligned_rectangles) {
@@ -823,4 +886,531 @@ OAPI uint64_t oracle_cpu_sort_fallback(const void* uni, const float* positions, 
         entries[2 * i + 1] = e[i].second;
     }
     return e.size();
+}
+
+// =============================================================================================
+// FP64 reference gradients and finite differences for the backward pass (test infrastructure).
+//
+// The differentiable function is the fp32 blend mode of the frame above, evaluated in FP64:
+// L = sum over pixels and RGB of (C - target)^2, with the depth order fixed by the FP32 keys of the
+// splat centres (as on the GPU).  Parameters per splat (59): centre 3, rotation 4 (used as given),
+// scale 3 (before splat_scale), opacity 1, SH 48.
+//   * oracle_grad_loss: full-frame loss and the analytic FP64 gradient — compositing backward
+//     back-to-front (suffix sums, no recomputation) and the vertex stage through FP64 dual numbers.
+//   * oracle_grad_fd: central difference of the loss in one parameter, re-rendering only the tiles
+//     the splat touches; returns 0 (excluded) when the perturbation changes anything discrete: the
+//     depth key, the set of tiles, or any pixel's list of contributing splats (coverage edge, 1/255
+//     discard, early stop).
+// =============================================================================================
+namespace {
+
+constexpr int NPARAM = 59;
+
+struct GRec {
+    double A00, A01, B0, A10, A11, B1, a, rgb[3], bx, by, R;
+    int x0, y0, x1, y1;  // inclusive pixel box; x0 > x1 when empty
+    bool valid;
+};
+
+struct GradCtx {
+    OU u;
+    OCfg cfg;
+    int W, H, TX, TY;
+    size_t n;
+    std::vector<double> c, q, s, a, sh, target;
+    std::vector<uint32_t> order, key;   // drawn splats in depth order, and their FP32 keys
+    std::vector<int64_t> pos_of;        // splat -> draw position (-1: not drawn)
+    std::vector<GRec> rec;              // per draw position
+    std::vector<std::vector<uint32_t>> tiles;  // per tile: draw positions, ascending
+};
+
+GRec make_rec(const GradCtx& g, const double* c, const double* q, const double* s, double a, const double* sh) {
+    VOut<double> o;
+    double shf[48];
+    const int nsh = 3 * (g.cfg.sh_order + 1) * (g.cfg.sh_order + 1);
+    for (int i = 0; i < 48; ++i) shf[i] = i < nsh ? sh[i] : 0.0;
+    vertex_core<double>(g.u, g.cfg, c, q, s, shf, o);
+    GRec r{};
+    r.A00 = o.A00; r.A01 = o.A01; r.B0 = o.B0; r.A10 = o.A10; r.A11 = o.A11; r.B1 = o.B1;
+    r.a = a;
+    for (int i = 0; i < 3; ++i) r.rgb[i] = o.rgb[i];
+    r.bx = o.bx; r.by = o.by;
+    const double vw = g.u.view_size[0], vh = g.u.view_size[1];
+    const double Wf = g.W, Hf = g.H;
+    const double sx = (2.0 * vw) / Wf, sy = -((2.0 * vh) / Hf);
+    const double m = g.u.margin;
+    double ex, ey;
+    r.R = 0.0;
+    if (g.cfg.use_unaligned_rectangles) {
+        ex = m * (std::fabs(o.Xx) + std::fabs(o.Yx));
+        ey = m * (std::fabs(o.Xy) + std::fabs(o.Yy));
+    } else {
+        r.R = std::sqrt(std::fmax(o.Xx * o.Xx + o.Xy * o.Xy, o.Yx * o.Yx + o.Yy * o.Yy)) * m;
+        ex = ey = r.R;
+    }
+    const double cxp = (o.Zx + vw) / sx, exq = ex / sx, cyp = (o.Zy - vh) / sy, eyq = ey / (-sy);
+    const double eps = 0.015625;
+    const double fx0 = std::ceil(cxp - exq - eps - 0.5), fx1 = std::floor(cxp + exq + eps - 0.5);
+    const double fy0 = std::ceil(cyp - eyq - eps - 0.5), fy1 = std::floor(cyp + eyq + eps - 0.5);
+    r.valid = std::isfinite(r.A00) && std::isfinite(r.A01) && std::isfinite(r.B0) && std::isfinite(r.A10) &&
+              std::isfinite(r.A11) && std::isfinite(r.B1) && std::isfinite(r.rgb[0]) && std::isfinite(r.rgb[1]) &&
+              std::isfinite(r.rgb[2]) && std::isfinite(fx0) && std::isfinite(fx1) && std::isfinite(fy0) &&
+              std::isfinite(fy1) && a >= 1.0 / 255.0;
+    r.x0 = 1; r.x1 = 0; r.y0 = 1; r.y1 = 0;
+    if (r.valid) {
+        const double cx0 = std::fmax(fx0, 0.0), cx1 = std::fmin(fx1, Wf - 1.0);
+        const double cy0 = std::fmax(fy0, 0.0), cy1 = std::fmin(fy1, Hf - 1.0);
+        if (cx0 <= cx1 && cy0 <= cy1) {
+            r.x0 = (int)cx0; r.x1 = (int)cx1; r.y0 = (int)cy0; r.y1 = (int)cy1;
+        }
+    }
+    return r;
+}
+
+GRec rec_of_splat(const GradCtx& g, size_t k, const double* override_params = nullptr) {
+    double p[NPARAM];
+    if (override_params) {
+        std::memcpy(p, override_params, sizeof(p));
+    } else {
+        for (int i = 0; i < 3; ++i) p[i] = g.c[3 * k + i];
+        for (int i = 0; i < 4; ++i) p[3 + i] = g.q[4 * k + i];
+        for (int i = 0; i < 3; ++i) p[7 + i] = g.s[3 * k + i];
+        p[10] = g.a[k];
+        for (int i = 0; i < 48; ++i) p[11 + i] = g.sh[48 * k + i];
+    }
+    return make_rec(g, p, p + 3, p + 7, p[10], p + 11);
+}
+
+struct Contrib {
+    uint32_t pos;
+    double alpha, E, tcx, tcy, s[3], sa, T;
+};
+
+// FP64 compositing of one pixel over the given draw positions; returns the contributors.
+void shade_pixel(const GradCtx& g, const GRec* recs, const uint32_t* list, size_t nl, int px, int py,
+                 std::vector<Contrib>* contribs, double* C, double* Tout) {
+    const double X = px + 0.5, Y = py + 0.5;
+    const double m = g.u.margin;
+    const double sx = (2.0 * g.u.view_size[0]) / g.W, sy = -((2.0 * g.u.view_size[1]) / g.H);
+    double T = 1.0;
+    C[0] = C[1] = C[2] = 0.0;
+    for (size_t li = 0; li < nl; ++li) {
+        const GRec& r = recs[li];
+        if (!r.valid || px < r.x0 || px > r.x1 || py < r.y0 || py > r.y1) continue;
+        const double tcx = r.A00 * X + r.A01 * Y + r.B0, tcy = r.A10 * X + r.A11 * Y + r.B1;
+        if (g.cfg.use_unaligned_rectangles) {
+            if (!(std::fabs(tcx) <= m && std::fabs(tcy) <= m)) continue;
+        } else {
+            const double dx = sx * X + r.bx, dy = sy * Y + r.by;
+            if (!(std::fabs(dx) <= r.R && std::fabs(dy) <= r.R)) continue;
+        }
+        const double E = std::exp(-0.5 * (tcx * tcx + tcy * tcy));
+        const double alpha = r.a * E;
+        if (alpha < 1.0 / 255.0) continue;
+        Contrib k;
+        k.pos = list[li];
+        k.alpha = alpha; k.E = E; k.tcx = tcx; k.tcy = tcy; k.T = T;
+        for (int ch = 0; ch < 3; ++ch) {
+            k.s[ch] = std::fmin(std::fmax(r.rgb[ch] * alpha, 0.0), 1.0);
+            C[ch] += k.s[ch] * T;
+        }
+        k.sa = std::fmin(std::fmax(alpha, 0.0), 1.0);
+        T = T * (1.0 - k.sa);
+        if (contribs) contribs->push_back(k);
+        if (T < 1e-4) break;
+    }
+    *Tout = T;
+}
+
+void atomic_add_d(std::atomic<uint64_t>* p, double v) {
+    uint64_t old = p->load(std::memory_order_relaxed), nw;
+    do {
+        double d;
+        std::memcpy(&d, &old, 8);
+        d += v;
+        std::memcpy(&nw, &d, 8);
+    } while (!p->compare_exchange_weak(old, nw, std::memory_order_relaxed));
+}
+
+}  // namespace
+
+OAPI void* oracle_grad_create(const void* uni, const void* cfgp, uint64_t n, const double* c, const double* q,
+                              const double* s, const double* a, const double* sh, const double* target) {
+    GradCtx* g = new GradCtx();
+    g->u = *(const OU*)uni;
+    g->cfg = *(const OCfg*)cfgp;
+    g->W = (int)g->u.image_size[0];
+    g->H = (int)g->u.image_size[1];
+    g->TX = (g->W + 15) / 16;
+    g->TY = (g->H + 15) / 16;
+    g->n = n;
+    g->c.assign(c, c + 3 * n);
+    g->q.assign(q, q + 4 * n);
+    g->s.assign(s, s + 3 * n);
+    g->a.assign(a, a + n);
+    g->sh.assign(sh, sh + 48 * n);
+    g->target.assign(target, target + 3 * (size_t)g->W * g->H);
+    std::vector<float> cf(3 * n);
+    for (size_t i = 0; i < 3 * n; ++i) cf[i] = (float)c[i];
+    std::vector<uint32_t> ek(n + 1), ei(n + 1);
+    uint64_t nv = 0, nd = 0;
+    oracle_draw_list(uni, g->cfg.depth_sorting, cf.data(), n, ek.data(), ei.data(), &nv, &nd);
+    g->order.assign(ei.begin(), ei.begin() + nd);
+    g->key.assign(ek.begin(), ek.begin() + nd);
+    g->pos_of.assign(n, -1);
+    for (size_t p = 0; p < nd; ++p) g->pos_of[g->order[p]] = (int64_t)p;
+    g->rec.resize(nd);
+    parallel_for((int64_t)nd, 16, [&](int64_t b, int64_t e) {
+        for (int64_t p = b; p < e; ++p) g->rec[p] = rec_of_splat(*g, g->order[p]);
+    });
+    g->tiles.assign((size_t)g->TX * g->TY, {});
+    for (size_t p = 0; p < nd; ++p) {
+        const GRec& r = g->rec[p];
+        if (!r.valid || r.x0 > r.x1) continue;
+        for (int ty = r.y0 / 16; ty <= r.y1 / 16; ++ty)
+            for (int tx = r.x0 / 16; tx <= r.x1 / 16; ++tx) g->tiles[(size_t)ty * g->TX + tx].push_back((uint32_t)p);
+    }
+    return g;
+}
+
+OAPI void oracle_grad_destroy(void* h) { delete (GradCtx*)h; }
+
+// Full-frame FP64 loss; grads (n x 59) receive the analytic FP64 gradient (zero for splats not drawn).
+OAPI double oracle_grad_loss_ex(void* h, double* grads, double* image_out, int threads, double* rec_grads_out,
+                                uint32_t* order_out);
+OAPI double oracle_grad_loss(void* h, double* grads, double* image_out, int threads) {
+    return oracle_grad_loss_ex(h, grads, image_out, threads, nullptr, nullptr);
+}
+// rec_grads_out (optional): per draw position, the 10 record gradients (d/dA against the pixel-centre
+// coordinates X = px + 0.5, Y = py + 0.5, d/dB, d/dopacity, d/drgb); order_out: splat index of each
+// draw position.
+OAPI double oracle_grad_loss_ex(void* h, double* grads, double* image_out, int threads, double* rec_grads_out,
+                                uint32_t* order_out) {
+    GradCtx& g = *(GradCtx*)h;
+    const size_t nd = g.order.size();
+    std::vector<std::atomic<uint64_t>> rg(nd * 10);
+    for (auto& x : rg) x.store(0);
+
+    std::atomic<int64_t> next{0};
+    std::vector<double> loss_t(threads > 0 ? threads : 1, 0.0);
+    auto worker = [&](int tid) {
+        std::vector<Contrib> cs;
+        std::vector<GRec> lrec;
+        for (;;) {
+            const int64_t t = next.fetch_add(1);
+            if (t >= (int64_t)g.tiles.size()) break;
+            const auto& L = g.tiles[t];
+            lrec.resize(L.size());
+            for (size_t i = 0; i < L.size(); ++i) lrec[i] = g.rec[L[i]];
+            const int tx = (int)(t % g.TX), ty = (int)(t / g.TX);
+            for (int py = ty * 16; py < std::min(g.H, ty * 16 + 16); ++py)
+                for (int px = tx * 16; px < std::min(g.W, tx * 16 + 16); ++px) {
+                    cs.clear();
+                    double C[3], Tf;
+                    shade_pixel(g, lrec.data(), L.data(), L.size(), px, py, &cs, C, &Tf);
+                    const size_t pix = (size_t)py * g.W + px;
+                    double gC[3];
+                    for (int ch = 0; ch < 3; ++ch) {
+                        const double d = C[ch] - g.target[3 * pix + ch];
+                        loss_t[tid] += d * d;
+                        gC[ch] = 2.0 * d;
+                        if (image_out) image_out[4 * pix + ch] = C[ch];
+                    }
+                    if (image_out) image_out[4 * pix + 3] = Tf;
+                    // back to front; S = colour of the splats behind
+                    double S[3] = {0.0, 0.0, 0.0};
+                    for (size_t ii = cs.size(); ii-- > 0;) {
+                        const Contrib& k = cs[ii];
+                        const GRec& r = g.rec[k.pos];
+                        double dS[3];
+                        for (int ch = 0; ch < 3; ++ch) dS[ch] = gC[ch] * k.T;
+                        const double om = 1.0 - k.sa;
+                        const double dsa = om > 0.0 ? -(gC[0] * S[0] + gC[1] * S[1] + gC[2] * S[2]) / om : 0.0;
+                        for (int ch = 0; ch < 3; ++ch) S[ch] += k.s[ch] * k.T;
+                        double dalpha = k.alpha < 1.0 ? dsa : 0.0;
+                        double out[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+                        for (int ch = 0; ch < 3; ++ch) {
+                            const double v = r.rgb[ch] * k.alpha;
+                            if (v > 0.0 && v < 1.0) {
+                                dalpha += dS[ch] * r.rgb[ch];
+                                out[7 + ch] = dS[ch] * k.alpha;
+                            }
+                        }
+                        out[6] = dalpha * k.E;
+                        const double dpow = -0.5 * dalpha * r.a * k.E;
+                        const double X = px + 0.5, Y = py + 0.5;
+                        const double dtx = 2.0 * dpow * k.tcx, dty = 2.0 * dpow * k.tcy;
+                        out[0] = dtx * X; out[1] = dtx * Y; out[2] = dtx;
+                        out[3] = dty * X; out[4] = dty * Y; out[5] = dty;
+                        for (int kk = 0; kk < 10; ++kk)
+                            if (out[kk] != 0.0) atomic_add_d(&rg[(size_t)k.pos * 10 + kk], out[kk]);
+
+                    }
+                }
+        }
+    };
+    const int nt = threads > 0 ? threads : 1;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker, t);
+    for (auto& th : pool) th.join();
+    double loss = 0.0;
+    for (double v : loss_t) loss += v;
+    if (rec_grads_out) {
+        for (size_t p = 0; p < nd; ++p) {
+            for (int kk = 0; kk < 10; ++kk) {
+                uint64_t bits = rg[p * 10 + kk].load();
+                std::memcpy(&rec_grads_out[p * 10 + kk], &bits, 8);
+            }
+            if (order_out) order_out[p] = g.order[p];
+        }
+    }
+    if (grads) {
+        std::memset(grads, 0, sizeof(double) * NPARAM * g.n);
+        parallel_for((int64_t)nd, nt, [&](int64_t b, int64_t e) {
+            for (int64_t p = b; p < e; ++p) {
+                double gr[10];
+                bool any = false;
+                for (int kk = 0; kk < 10; ++kk) {
+                    const uint64_t bits = rg[(size_t)p * 10 + kk].load();
+                    std::memcpy(&gr[kk], &bits, 8);
+                    any = any || gr[kk] != 0.0;
+                }
+                if (!any) continue;
+                const size_t k = g.order[p];
+                double* out = grads + NPARAM * k;
+                // vertex stage through dual numbers: one pass per centre/rotation/scale direction
+                Dd shd[48];
+                const int nsh = 3 * (g.cfg.sh_order + 1) * (g.cfg.sh_order + 1);
+                for (int i = 0; i < 48; ++i) shd[i] = Dd(i < nsh ? g.sh[48 * k + i] : 0.0);
+                for (int dir = 0; dir < 10; ++dir) {
+                    Dd cc[3], qq[4], ss[3];
+                    for (int i = 0; i < 3; ++i) cc[i] = Dd(g.c[3 * k + i], dir == i ? 1.0 : 0.0);
+                    for (int i = 0; i < 4; ++i) qq[i] = Dd(g.q[4 * k + i], dir == 3 + i ? 1.0 : 0.0);
+                    for (int i = 0; i < 3; ++i) ss[i] = Dd(g.s[3 * k + i], dir == 7 + i ? 1.0 : 0.0);
+                    VOut<Dd> o;
+                    vertex_core<Dd>(g.u, g.cfg, cc, qq, ss, shd, o);
+                    out[dir] = gr[0] * o.A00.d + gr[1] * o.A01.d + gr[2] * o.B0.d + gr[3] * o.A10.d +
+                               gr[4] * o.A11.d + gr[5] * o.B1.d + gr[7] * o.rgb[0].d + gr[8] * o.rgb[1].d +
+                               gr[9] * o.rgb[2].d;
+                }
+                out[10] = gr[6];
+                // SH coefficients enter linearly: basis value times the colour gradient
+                double cc[3] = {g.c[3 * k], g.c[3 * k + 1], g.c[3 * k + 2]};
+                double v[3], d[3];
+                for (int i = 0; i < 3; ++i) v[i] = cc[i] - (double)g.u.camera[12 + i];
+                const double len = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                for (int i = 0; i < 3; ++i) d[i] = v[i] / len;
+                const int nk = (g.cfg.sh_order + 1) * (g.cfg.sh_order + 1);
+                for (int kk = 0; kk < nk; ++kk) {
+                    double one[48] = {0.0};
+                    one[3 * kk] = 1.0;
+                    double rgb[3];
+                    sh_lookup(d, one, g.cfg.sh_order, rgb);
+                    const double basis = rgb[0] - 0.5;
+                    for (int ch = 0; ch < 3; ++ch) out[11 + 3 * kk + ch] = basis * gr[7 + ch];
+                }
+            }
+        });
+    }
+    return loss;
+}
+
+// FP64 Jacobian of splat k's record (A00, A01, B0, A10, A11, B1, r, g, b; A against pixel-centre
+// coordinates) with respect to its centre, rotation and scale (10 directions): J[dir * 9 + out].
+OAPI void oracle_grad_jacobian(void* h, uint64_t k, double* J) {
+    GradCtx& g = *(GradCtx*)h;
+    Dd shd[48];
+    const int nsh = 3 * (g.cfg.sh_order + 1) * (g.cfg.sh_order + 1);
+    for (int i = 0; i < 48; ++i) shd[i] = Dd(i < nsh ? g.sh[48 * k + i] : 0.0);
+    for (int dir = 0; dir < 10; ++dir) {
+        Dd cc[3], qq[4], ss[3];
+        for (int i = 0; i < 3; ++i) cc[i] = Dd(g.c[3 * k + i], dir == i ? 1.0 : 0.0);
+        for (int i = 0; i < 4; ++i) qq[i] = Dd(g.q[4 * k + i], dir == 3 + i ? 1.0 : 0.0);
+        for (int i = 0; i < 3; ++i) ss[i] = Dd(g.s[3 * k + i], dir == 7 + i ? 1.0 : 0.0);
+        VOut<Dd> o;
+        vertex_core<Dd>(g.u, g.cfg, cc, qq, ss, shd, o);
+        const double v[9] = {o.A00.d, o.A01.d, o.B0.d, o.A10.d, o.A11.d, o.B1.d, o.rgb[0].d, o.rgb[1].d, o.rgb[2].d};
+        for (int j = 0; j < 9; ++j) J[dir * 9 + j] = v[j];
+    }
+}
+
+// Central difference of the loss in parameter `param` (0..58) of splat k with step hstep.  Returns 1
+// and writes *fd when nothing discrete changes under +-hstep, 0 otherwise (excluded).
+OAPI int oracle_grad_fd(void* h, uint64_t k, int param, double hstep, double* fd) {
+    GradCtx& g = *(GradCtx*)h;
+    *fd = 0.0;
+    if (g.pos_of[k] < 0) return 0;
+    const uint32_t pos = (uint32_t)g.pos_of[k];
+    double base[NPARAM];
+    for (int i = 0; i < 3; ++i) base[i] = g.c[3 * k + i];
+    for (int i = 0; i < 4; ++i) base[3 + i] = g.q[4 * k + i];
+    for (int i = 0; i < 3; ++i) base[7 + i] = g.s[3 * k + i];
+    base[10] = g.a[k];
+    for (int i = 0; i < 48; ++i) base[11 + i] = g.sh[48 * k + i];
+    GRec rr[2];
+    for (int sgn = 0; sgn < 2; ++sgn) {
+        double p[NPARAM];
+        std::memcpy(p, base, sizeof(p));
+        p[param] += sgn == 0 ? hstep : -hstep;
+        if (param < 3) {  // the FP32 depth key (and culling) must not change
+            float cf[3] = {(float)p[0], (float)p[1], (float)p[2]};
+            uint32_t kk;
+            uint8_t vis;
+            oracle_cull_keys(&g.u, g.cfg.depth_sorting, cf, 1, &kk, &vis);
+            if (!vis || kk != g.key[pos]) return 0;
+        }
+        rr[sgn] = rec_of_splat(g, k, p);
+        if (!rr[sgn].valid) return 0;
+    }
+    const GRec& r0 = g.rec[pos];
+    auto tiles_of = [&](const GRec& r, std::vector<int64_t>& out) {
+        if (!r.valid || r.x0 > r.x1) return;
+        for (int ty = r.y0 / 16; ty <= r.y1 / 16; ++ty)
+            for (int tx = r.x0 / 16; tx <= r.x1 / 16; ++tx) out.push_back((int64_t)ty * g.TX + tx);
+    };
+    std::vector<int64_t> t0, tp, tm;
+    tiles_of(r0, t0);
+    tiles_of(rr[0], tp);
+    tiles_of(rr[1], tm);
+    if (t0 != tp || t0 != tm) return 0;  // the splat enters or leaves a tile
+    double loss[2] = {0.0, 0.0};
+    for (int64_t t : t0) {
+        const auto& L = g.tiles[t];
+        std::vector<GRec> lrec(L.size());
+        const int tx = (int)(t % g.TX), ty = (int)(t / g.TX);
+        std::vector<std::vector<uint32_t>> sig(2);
+        for (int sgn = 0; sgn < 2; ++sgn) {
+            for (size_t i = 0; i < L.size(); ++i) lrec[i] = L[i] == pos ? rr[sgn] : g.rec[L[i]];
+            std::vector<Contrib> cs;
+            for (int py = ty * 16; py < std::min(g.H, ty * 16 + 16); ++py)
+                for (int px = tx * 16; px < std::min(g.W, tx * 16 + 16); ++px) {
+                    cs.clear();
+                    double C[3], Tf;
+                    shade_pixel(g, lrec.data(), L.data(), L.size(), px, py, &cs, C, &Tf);
+                    const size_t pix = (size_t)py * g.W + px;
+                    for (int ch = 0; ch < 3; ++ch) {
+                        const double d = C[ch] - g.target[3 * pix + ch];
+                        loss[sgn] += d * d;
+                    }
+                    for (auto& c : cs) sig[sgn].push_back(c.pos);
+                    sig[sgn].push_back(0xFFFFFFFFu);
+                }
+        }
+        if (sig[0] != sig[1]) return 0;
+    }
+    *fd = (loss[0] - loss[1]) / (2.0 * hstep);
+    return 1;
+}
+
+// Splats whose gradient depends on a decision that the FP32 frame and the FP64 frame take
+// differently: for every pixel, the FP32 contributors (the GPU's frame, bit for bit: same records,
+// coverage, falloff, 1/255 discard, early stop) and their saturation regimes are compared with the
+// FP64 ones; every splat contributing to a pixel where they differ is flagged (1).  Gradients of
+// flagged splats differ between FP32 and FP64 by construction (a threshold is crossed within
+// rounding), so comparisons exclude them.  Returns the number of differing pixels.
+OAPI uint64_t oracle_grad_ambiguous(void* h, uint8_t* flags, int threads) {
+    GradCtx& g = *(GradCtx*)h;
+    const size_t nd = g.order.size();
+    // FP32 records of the drawn entries, exactly as the GPU computes them
+    std::vector<float> rec32(16 * nd);
+    parallel_for((int64_t)nd, threads, [&](int64_t b, int64_t e) {
+        for (int64_t p = b; p < e; ++p) {
+            const size_t k = g.order[p];
+            float c[3], q[4], s[3], sh[48];
+            for (int i = 0; i < 3; ++i) c[i] = (float)g.c[3 * k + i];
+            for (int i = 0; i < 4; ++i) q[i] = (float)g.q[4 * k + i];
+            for (int i = 0; i < 3; ++i) s[i] = (float)g.s[3 * k + i];
+            for (int i = 0; i < 48; ++i) sh[i] = (float)g.sh[48 * k + i];
+            preprocess_one<float>(g.u, g.cfg, c, q, s, (float)g.a[k], sh, rec32.data() + 16 * p, nullptr);
+        }
+    });
+    // FP32 tile lists (the GPU bins with the FP32 boxes)
+    std::vector<std::vector<uint32_t>> tl32((size_t)g.TX * g.TY);
+    for (size_t p = 0; p < nd; ++p) {
+        const float* rc = rec32.data() + 16 * p;
+        const uint32_t lo = float_to_bits(rc[7]), hi = float_to_bits(rc[11]);
+        const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16), x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
+        if (x0 > x1 || y0 > y1) continue;
+        for (int ty = y0 / 16; ty <= y1 / 16; ++ty)
+            for (int tx = x0 / 16; tx <= x1 / 16; ++tx) tl32[(size_t)ty * g.TX + tx].push_back((uint32_t)p);
+    }
+    std::vector<std::atomic<uint8_t>> fl(g.n);
+    for (auto& f : fl) f.store(0);
+    std::atomic<uint64_t> npix{0};
+    std::atomic<int64_t> next{0};
+    const float m = g.u.margin;
+    auto worker = [&] {
+        std::vector<Contrib> cs;
+        std::vector<GRec> lrec;
+        std::vector<uint64_t> s32, s64;
+        for (;;) {
+            const int64_t t = next.fetch_add(1);
+            if (t >= (int64_t)g.tiles.size()) break;
+            const auto& L64 = g.tiles[t];
+            const auto& L32 = tl32[t];
+            lrec.resize(L64.size());
+            for (size_t i = 0; i < L64.size(); ++i) lrec[i] = g.rec[L64[i]];
+            const int tx = (int)(t % g.TX), ty = (int)(t / g.TX);
+            for (int py = ty * 16; py < std::min(g.H, ty * 16 + 16); ++py)
+                for (int px = tx * 16; px < std::min(g.W, tx * 16 + 16); ++px) {
+                    // FP32 frame
+                    s32.clear();
+                    const float X = (float)px + 0.5f, Y = (float)py + 0.5f;
+                    float ft = 1.0f;
+                    for (uint32_t p : L32) {
+                        const float* rc = rec32.data() + 16 * (size_t)p;
+                        const uint32_t lo = float_to_bits(rc[7]), hi = float_to_bits(rc[11]);
+                        if (px < (int)(lo & 0xFFFFu) || px > (int)(hi & 0xFFFFu) || py < (int)(lo >> 16) ||
+                            py > (int)(hi >> 16))
+                            continue;
+                        const float tcx = std::fmaf(rc[1], Y, std::fmaf(rc[0], X, rc[2]));
+                        const float tcy = std::fmaf(rc[4], Y, std::fmaf(rc[3], X, rc[5]));
+                        if (g.cfg.use_unaligned_rectangles) {
+                            if (!(std::fabs(tcx) <= m && std::fabs(tcy) <= m)) continue;
+                        } else {
+                            const float sx = (2.0f * g.u.view_size[0]) / (float)g.W;
+                            const float sy = -((2.0f * g.u.view_size[1]) / (float)g.H);
+                            const float dx = std::fmaf(sx, X, rc[12]), dy = std::fmaf(sy, Y, rc[13]);
+                            if (!(std::fabs(dx) <= rc[14] && std::fabs(dy) <= rc[14])) continue;
+                        }
+                        const float alpha = rc[6] * o_expf(-0.5f * std::fmaf(tcx, tcx, tcy * tcy));
+                        if (alpha < ALPHA_MIN) continue;
+                        uint64_t regime = 0;
+                        for (int ch = 0; ch < 3; ++ch) {
+                            const float v = rc[8 + ch] * alpha;
+                            regime |= (uint64_t)(v > 0.0f && v < 1.0f) << ch;
+                        }
+                        regime |= (uint64_t)(alpha < 1.0f) << 3;
+                        s32.push_back(((uint64_t)p << 4) | regime);
+                        ft = ft * (1.0f - clamp01(alpha));
+                        if (ft < FP32_T_MIN) break;
+                    }
+                    // FP64 frame
+                    cs.clear();
+                    double C[3], Tf;
+                    shade_pixel(g, lrec.data(), L64.data(), L64.size(), px, py, &cs, C, &Tf);
+                    s64.clear();
+                    for (auto& k : cs) {
+                        const GRec& r = g.rec[k.pos];
+                        uint64_t regime = 0;
+                        for (int ch = 0; ch < 3; ++ch) {
+                            const double v = r.rgb[ch] * k.alpha;
+                            regime |= (uint64_t)(v > 0.0 && v < 1.0) << ch;
+                        }
+                        regime |= (uint64_t)(k.alpha < 1.0) << 3;
+                        s64.push_back(((uint64_t)k.pos << 4) | regime);
+                    }
+                    if (s32 != s64) {
+                        ++npix;
+                        for (uint64_t v : s32) fl[g.order[v >> 4]].store(1);
+                        for (uint64_t v : s64) fl[g.order[v >> 4]].store(1);
+                    }
+                }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < (threads > 0 ? threads : 1); ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+    for (size_t i = 0; i < g.n; ++i) flags[i] = fl[i].load();
+    return npix.load();
 }

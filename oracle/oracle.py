@@ -13,7 +13,7 @@ from . import build_oracle
 
 __all__ = [
     "lib", "uniforms", "cull_keys", "draw_list", "preprocess", "raster", "render", "load_transform",
-    "cpu_sort_fallback", "cpu_frame_timed", "expf", "OCFG", "UNIFORM_DTYPE", "config_struct",
+    "cpu_sort_fallback", "cpu_frame_timed", "expf", "GradContext", "OCFG", "UNIFORM_DTYPE", "config_struct",
 ]
 
 _lib = None
@@ -196,3 +196,82 @@ def cpu_sort_fallback(u, positions):
     ent = np.empty((max(n, 1), 2), np.uint32)
     v = lib().oracle_cpu_sort_fallback(_p(u), _p(p), n, _p(ent))
     return ent[:v]
+
+
+class GradContext:
+    """FP64 reference gradients and finite differences of the fp32-blend frame (TEST INFRASTRUCTURE).
+
+    Parameters per splat (59): centre 3, rotation 4 (as given), scale 3, opacity 1, SH 48.  The loss is
+    sum over pixels and RGB of (C - target)^2; target is (H, W, 3) float64."""
+
+    NPARAM = 59
+
+    def __init__(self, u, cfg, scene64, target):
+        L = lib()
+        if not hasattr(L, "_grad_bound"):
+            P = ctypes.c_void_p
+            L.oracle_grad_create.restype = P
+            L.oracle_grad_create.argtypes = [P, P, ctypes.c_uint64, P, P, P, P, P, P]
+            L.oracle_grad_destroy.restype = None
+            L.oracle_grad_destroy.argtypes = [P]
+            L.oracle_grad_loss.restype = ctypes.c_double
+            L.oracle_grad_loss.argtypes = [P, P, P, ctypes.c_int]
+            L.oracle_grad_fd.restype = ctypes.c_int
+            L.oracle_grad_fd.argtypes = [P, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, P]
+            L.oracle_grad_jacobian.restype = None
+            L.oracle_grad_jacobian.argtypes = [P, ctypes.c_uint64, P]
+            L.oracle_grad_loss_ex.restype = ctypes.c_double
+            L.oracle_grad_loss_ex.argtypes = [P, P, P, ctypes.c_int, P, P]
+            L.oracle_grad_ambiguous.restype = ctypes.c_uint64
+            L.oracle_grad_ambiguous.argtypes = [P, P, ctypes.c_int]
+            L._grad_bound = True
+        self._keep = [np.ascontiguousarray(scene64[k], np.float64) for k in ("center", "rotation", "scale", "alpha",
+                                                                             "sh")]
+        self.n = self._keep[0].shape[0]
+        self.W, self.H = (int(x) for x in u["image_size"][0])
+        tgt = np.ascontiguousarray(target, np.float64).reshape(self.H, self.W, 3)
+        self._h = L.oracle_grad_create(_p(u), _p(cfg), self.n, *(_p(a) for a in self._keep), _p(tgt))
+
+    def loss_and_grad(self, threads=8):
+        grads = np.zeros((self.n, self.NPARAM), np.float64)
+        image = np.zeros((self.H, self.W, 4), np.float64)
+        loss = lib().oracle_grad_loss(self._h, _p(grads), _p(image), int(threads))
+        return loss, grads, image
+
+    def record_gradients(self, threads=8):
+        """(per draw position the 10 record gradients, A against pixel-centre coordinates; splat index
+        of each draw position)."""
+        nd = self.n
+        rg = np.zeros((nd, 10), np.float64)
+        order = np.zeros(nd, np.uint32)
+        lib().oracle_grad_loss_ex(self._h, None, None, int(threads), _p(rg), _p(order))
+        return rg, order
+
+    def jacobian(self, k):
+        """(10, 9) FP64 Jacobian of splat k's record (A00, A01, B0, A10, A11, B1, r, g, b; A against
+        pixel-centre coordinates) in its centre, rotation and scale."""
+        J = np.zeros((10, 9), np.float64)
+        lib().oracle_grad_jacobian(self._h, int(k), _p(J))
+        return J
+
+    def ambiguous(self, threads=8):
+        """(flags per splat, #pixels) where the FP32 frame and the FP64 frame differ in a decision."""
+        flags = np.zeros(self.n, np.uint8)
+        npix = lib().oracle_grad_ambiguous(self._h, _p(flags), int(threads))
+        return flags.astype(bool), int(npix)
+
+    def fd(self, k, param, h=1e-4):
+        out = np.zeros(1, np.float64)
+        ok = lib().oracle_grad_fd(self._h, int(k), int(param), float(h), _p(out))
+        return bool(ok), float(out[0])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().oracle_grad_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,131 @@
+"""Differentiable rendering: torch.autograd.Function over the hand-written backward kernels.
+
+`render_splats` takes the splat parameters the renderer uses (centres, rotations as given, scales,
+opacities, SH) and returns the float4 image of an fp32-blend frame; its backward calls
+spl_render_backward (raster backward + vertex-stage backward on the GPU).  `render_raw` applies the
+file loader's activations first (Scene::load_chunk, scene.rs:225-250: rotor normalisation, exp of the
+log-scales clamped to mean +- 5, sigmoid of the opacity logit), so gradients reach the raw
+parameters a training loop optimises.  Depth order, culling and the 1/255 discard are constants of
+the frame (no gradient), as in any splat rasteriser.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .renderer import BlendMode, Renderer, _stream_ptr
+
+__all__ = ["render_splats", "render_raw", "activate"]
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class _WrappedScene:
+    """A scene over caller-owned device tensors (spl_scene_wrap); keeps the tensors alive."""
+
+    def __init__(self, renderer, xyz, rot, scale_alpha, sh):
+        self._lib = _lib.load()
+        self._keep = (xyz, rot, scale_alpha, sh)
+        n = rot.shape[0]
+        h = ctypes.c_void_p()
+        check(self._lib.spl_scene_wrap(renderer.handle, n, _ptr(xyz[0]), _ptr(xyz[1]), _ptr(xyz[2]), _ptr(rot),
+                                       _ptr(scale_alpha), _ptr(sh), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.spl_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _import_torch():
+    import torch
+    return torch
+
+
+class _RenderSplats:  # built lazily so that importing the package does not import torch
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is None:
+            torch = _import_torch()
+
+            class RenderSplats(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, xyz, rot, scale_alpha, sh, renderer, camera_to_world, width, height):
+                    xyz = xyz.contiguous()
+                    rot = rot.contiguous()
+                    scale_alpha = scale_alpha.contiguous()
+                    sh = sh.contiguous()
+                    scene = _WrappedScene(renderer, xyz, rot, scale_alpha, sh)
+                    img = renderer.render_frame(scene, camera_to_world, width, height)
+                    ctx.renderer = renderer
+                    ctx.scene = scene
+                    ctx.cam = np.ascontiguousarray(np.asarray(camera_to_world, np.float32).reshape(16))
+                    ctx.size = (width, height)
+                    ctx.save_for_backward(img)
+                    renderer._last_frame_key = (id(scene), ctx.cam.tobytes(), width, height)
+                    return img
+
+                @staticmethod
+                def backward(ctx, grad_img):
+                    (img,) = ctx.saved_tensors
+                    r = ctx.renderer
+                    w, h = ctx.size
+                    key = (id(ctx.scene), ctx.cam.tobytes(), w, h)
+                    if getattr(r, "_last_frame_key", None) != key:
+                        # another frame was rendered since: re-render this one (deterministic)
+                        r.render_frame(ctx.scene, ctx.cam, w, h)
+                        r._last_frame_key = key
+                    xyz, rot, sa, sh = ctx.scene._keep
+                    gxyz = torch.zeros_like(xyz)
+                    grot = torch.zeros_like(rot)
+                    gsa = torch.zeros_like(sa)
+                    gsh = torch.zeros_like(sh)
+                    g = grad_img.contiguous().float()
+                    check(r._lib.spl_render_backward(r.handle, ctx.scene.handle, _ptr(img), _ptr(g), _ptr(gxyz[0]),
+                                                     _ptr(gxyz[1]), _ptr(gxyz[2]), _ptr(grot), _ptr(gsa), _ptr(gsh),
+                                                     _stream_ptr(None)))
+                    return gxyz, grot, gsa, gsh, None, None, None, None
+
+            cls.fn = RenderSplats
+        return cls.fn
+
+
+def render_splats(xyz, rotation, scale_alpha, sh, renderer: Renderer, camera_to_world, width, height):
+    """Differentiable frame.  xyz: (3, N) centre planes; rotation: (N, 4) scalar first; scale_alpha:
+    (N, 4) scale xyz + opacity; sh: (N, 48).  Returns (H, W, 4) float32 (r, g, b, T)."""
+    if renderer.config.blend_mode != BlendMode.FP32:
+        raise ValueError("render_splats needs a renderer with blend_mode FP32")
+    return _RenderSplats.get().apply(xyz, rotation, scale_alpha, sh, renderer, camera_to_world, width, height)
+
+
+def activate(means, quats, log_scales, opacity_logits):
+    """The loader's activations (scene.rs:225-250) in torch: (xyz planes, rotation, scale_alpha)."""
+    torch = _import_torch()
+    rot = quats * (1.0 / torch.sqrt((quats * quats).sum(-1, keepdim=True)))
+    avg = log_scales.sum(-1, keepdim=True) / 3.0
+    ls = torch.minimum(torch.maximum(log_scales, avg - 5.0), avg + 5.0)
+    scale = torch.exp(ls)
+    alpha = torch.sigmoid(opacity_logits)
+    return means.t(), rot, torch.cat([scale, alpha[:, None]], 1)
+
+
+def render_raw(means, quats, log_scales, opacity_logits, sh, renderer, camera_to_world, width, height):
+    """Differentiable frame from raw parameters (positions, quaternions, log-scales, opacity logits, SH)."""
+    xyz, rot, sa = activate(means, quats, log_scales, opacity_logits)
+    return render_splats(xyz, rot, sa, sh, renderer, camera_to_world, width, height)

@@ -143,13 +143,16 @@ struct spl_renderer {
     uint32_t last_w = 0, last_h = 0;
     uint64_t last_n = 0;
     const uint32_t* final_pair_vals = nullptr;
+    const spl_scene* last_scene = nullptr;
+    Uniforms last_u{};
+    float* grad_rec = nullptr;  // [max_n][10] record gradients of the backward pass (allocated on first use)
     // stage profiling: events 0..7 on the frame's stream
     bool profiling = false;
     cudaEvent_t ev_prof[8] = {};
 
 
     void release() {
-        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes);
+        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes); dfree(grad_rec);
         dfree(st_cull); dfree(st_bin);
         dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b);
         dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges);
@@ -176,6 +179,7 @@ struct spl_scene {
     spl_renderer* renderer = nullptr;
     int device = 0;
     uint64_t n = 0;
+    bool owns = true;  // false for scenes wrapping caller-owned arrays (spl_scene_wrap)
     float *x = nullptr, *y = nullptr, *z = nullptr, *sh = nullptr;
     float4 *rot = nullptr, *scale_alpha = nullptr;
     Staging stg;
@@ -183,7 +187,9 @@ struct spl_scene {
 
     SceneView view() const { return SceneView{x, y, z, rot, scale_alpha, sh, (uint32_t)n}; }
     void release() {
-        dfree(x); dfree(y); dfree(z); dfree(sh); dfree(rot); dfree(scale_alpha);
+        if (owns) {
+            dfree(x); dfree(y); dfree(z); dfree(sh); dfree(rot); dfree(scale_alpha);
+        }
         for (int i = 0; i < 2; ++i) {
             if (stg.pinned[i]) cudaFreeHost(stg.pinned[i]);
             dfree(stg.dev[i]);
@@ -443,6 +449,8 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     r->mark(7, st);
     CU(cudaGetLastError());
     r->last_stream = st;
+    r->last_scene = scene;
+    r->last_u = u;
     r->has_frame = true;
     r->last_w = width;
     r->last_h = height;
@@ -485,6 +493,40 @@ int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint3
     // frame_begin, cull, preprocess, depth sort (one cooperative launch), ranges memset, bin,
     // pair sort (one cooperative launch), ranges, raster
     return 1 + 1 + 1 + depth_sort + 1 + 1 + 1 + 1 + 1;
+}
+
+int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
+                        const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z, float* grad_rotation,
+                        float* grad_scale_alpha, float* grad_sh, void* stream) {
+    if (!r || !scene || !image_device || !grad_image_device || !grad_x || !grad_y || !grad_z || !grad_rotation ||
+        !grad_scale_alpha || !grad_sh)
+        return fail(SPL_ERR_INVALID, "NULL argument");
+    if (r->cfg.blend_mode != SPL_BLEND_FP32) return fail(SPL_ERR_INVALID, "the backward pass needs blend_mode FP32");
+    if (!r->has_frame || r->last_scene != scene)
+        return fail(SPL_ERR_INVALID, "render this scene with spl_render_frame first (the backward reuses that frame)");
+    if (!r->grad_rec) {
+        int rc = dalloc(&r->grad_rec, r->max_n * 10);
+        if (rc) return rc;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const spl_config& cfg = r->cfg;
+    launch_backward((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
+                    cfg.use_unaligned_rectangles != 0, scene->view(), r->last_u, r->idx, r->fc, r->boxes, r->ranges,
+                    r->final_pair_vals, r->rec, reinterpret_cast<const float4*>(image_device),
+                    reinterpret_cast<const float4*>(grad_image_device), r->grad_rec, (uint32_t)scene->n, grad_x,
+                    grad_y, grad_z, reinterpret_cast<float4*>(grad_rotation), reinterpret_cast<float4*>(grad_scale_alpha),
+                    grad_sh, st);
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
+int spl_renderer_copy_record_gradients(spl_renderer* r, float* dst_device, uint64_t capacity, void* stream) {
+    if (!r || !dst_device) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (!r->grad_rec) return fail(SPL_ERR_INVALID, "no backward pass has run on this renderer");
+    if (capacity > r->max_n) capacity = r->max_n;
+    if (capacity == 0) return SPL_OK;
+    CU(cudaMemcpyAsync(dst_device, r->grad_rec, capacity * 40, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return SPL_OK;
 }
 
 int spl_renderer_frame_info(spl_renderer* r, spl_frame_info* info) {
@@ -628,6 +670,29 @@ void spl_scene_destroy(spl_scene* s) {
 }
 
 uint64_t spl_scene_splat_count(const spl_scene* s) { return s ? s->n : 0; }
+
+int spl_scene_wrap(spl_renderer* r, uint64_t splat_count, float* x, float* y, float* z, float* rotation,
+                   float* scale_alpha, float* sh, spl_scene** out) {
+    if (!r || !out || !x || !y || !z || !rotation || !scale_alpha || !sh) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (splat_count > r->max_n) return fail(SPL_ERR_INVALID, "splat_count above max_splat_count");
+    if ((reinterpret_cast<uintptr_t>(rotation) | reinterpret_cast<uintptr_t>(scale_alpha) |
+         reinterpret_cast<uintptr_t>(sh)) & 15u)
+        return fail(SPL_ERR_INVALID, "rotation, scale_alpha and sh must be 16-byte aligned");
+    spl_scene* s = new (std::nothrow) spl_scene();
+    if (!s) return fail(SPL_ERR_OOM, "host allocation failed");
+    s->renderer = r;
+    cudaGetDevice(&s->device);
+    s->n = splat_count;
+    s->owns = false;
+    s->x = x;
+    s->y = y;
+    s->z = z;
+    s->rot = reinterpret_cast<float4*>(rotation);
+    s->scale_alpha = reinterpret_cast<float4*>(scale_alpha);
+    s->sh = sh;
+    *out = s;
+    return SPL_OK;
+}
 uint64_t spl_scene_device_bytes(const spl_scene* s) { return s ? s->n * 236ull : 0; }
 
 int spl_scene_load_chunk(spl_scene* s, const void* records, uint64_t start, uint64_t count, void* stream) {

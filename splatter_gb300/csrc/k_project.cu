@@ -12,7 +12,7 @@
 // bit-identical to the oracle's FP32 restatement.
 #include <cstdio>
 
-#include "spl_device.cuh"
+#include "spl_vertex.cuh"
 
 namespace spl {
 
@@ -158,113 +158,6 @@ void launch_cull_key(int mode, const SceneView& s, const Uniforms& u, FrameCount
 }
 
 // ------------------------------------------------------------------------------------------------
-// Vertex-stage math (shaders.wgsl), FP32, in the WGSL operation order.
-struct M3 {
-    float m[9];  // column-major m[c*3 + r]
-};
-
-__device__ __forceinline__ M3 mul3(const M3& A, const M3& B) {
-    M3 t;
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-            t.m[j * 3 + i] = (A.m[0 * 3 + i] * B.m[j * 3 + 0] + A.m[1 * 3 + i] * B.m[j * 3 + 1]) + A.m[2 * 3 + i] * B.m[j * 3 + 2];
-    return t;
-}
-__device__ __forceinline__ M3 transpose3(const M3& A) {
-    M3 t;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int r = 0; r < 3; ++r) t.m[c * 3 + r] = A.m[r * 3 + c];
-    return t;
-}
-
-// quatToMat (shaders.wgsl:63-79)
-__device__ __forceinline__ M3 quat_to_mat(float4 p) {
-    const float s2 = 1.41421356237309504880f;
-    const float qx = p.x * s2, qy = p.y * s2, qz = p.z * s2, qw = p.w * s2;
-    const float yy = qy * qy, yz = qy * qz, yw = qy * qw, yx = qy * qx;
-    const float zz = qz * qz, zw = qz * qw, zx = qz * qx;
-    const float ww = qw * qw, wx = qw * qx;
-    M3 m;
-    m.m[0] = (1.0f - zz) - ww; m.m[1] = yz + wx;          m.m[2] = yw - zx;
-    m.m[3] = yz - wx;          m.m[4] = (1.0f - yy) - ww; m.m[5] = zw + yx;
-    m.m[6] = yw + zx;          m.m[7] = zw - yx;          m.m[8] = (1.0f - yy) - zz;
-    return m;
-}
-
-__device__ __forceinline__ M3 camera3(const Uniforms& u) {
-    M3 c;
-#pragma unroll
-    for (int col = 0; col < 3; ++col)
-#pragma unroll
-        for (int r = 0; r < 3; ++r) c.m[col * 3 + r] = u.camera[col * 4 + r];
-    return c;
-}
-
-// projectedContourOfEllipsoid (shaders.wgsl:125-169)
-__device__ __forceinline__ M3 projected_contour(const Uniforms& u, float sx, float sy, float sz, float4 rot, float tx,
-                                                float ty, float tz) {
-    const M3 C = camera3(u);
-    M3 T = quat_to_mat(rot);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        T.m[0 * 3 + r] = T.m[0 * 3 + r] / sx;
-        T.m[1 * 3 + r] = T.m[1 * 3 + r] / sy;
-        T.m[2 * 3 + r] = T.m[2 * 3 + r] / sz;
-    }
-    const float ro0 = u.camera[12] - tx, ro1 = u.camera[13] - ty, ro2 = u.camera[14] - tz;
-    float l[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) l[i] = (ro0 * T.m[i * 3 + 0] + ro1 * T.m[i * 3 + 1]) + ro2 * T.m[i * 3 + 2];
-    const float l0 = l[0] * l[0], l1 = l[1] * l[1], l2 = l[2] * l[2];
-    const float dx = (1.0f - l1) - l2, dy = (1.0f - l0) - l2, dz = (1.0f - l0) - l1;
-    const float trx = l[1] * l[2], try_ = l[0] * l[2], trz = l[0] * l[1];
-    M3 A;
-    A.m[0] = dx;   A.m[1] = trz;  A.m[2] = try_;
-    A.m[3] = trz;  A.m[4] = dy;   A.m[5] = trx;
-    A.m[6] = try_; A.m[7] = trx;  A.m[8] = dz;
-    const M3 T2 = mul3(transpose3(C), T);
-    return mul3(mul3(T2, A), transpose3(T2));
-}
-
-// projectedCovarianceOfEllipsoid (shaders.wgsl:99-118)
-__device__ __forceinline__ M3 projected_covariance(const Uniforms& u, float sx, float sy, float sz, float4 rot,
-                                                   float tx, float ty, float tz) {
-    const M3 C = camera3(u);
-    M3 T = quat_to_mat(rot);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        T.m[0 * 3 + r] = T.m[0 * 3 + r] * sx;
-        T.m[1 * 3 + r] = T.m[1 * 3 + r] * sy;
-        T.m[2 * 3 + r] = T.m[2 * 3 + r] * sz;
-    }
-    float v[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-        v[r] = ((u.view[0 * 4 + r] * tx + u.view[1 * 4 + r] * ty) + u.view[2 * 4 + r] * tz) + u.view[3 * 4 + r] * 1.0f;
-    v[0] = fminf(fmaxf(v[0] / v[2], -1.0f), 1.0f) * v[2];
-    v[1] = fminf(fmaxf(v[1] / v[2], -1.0f), 1.0f) * v[2];
-    const float zz = v[2] * v[2];
-    M3 J;
-    J.m[0] = 1.0f / v[2]; J.m[1] = 0.0f;        J.m[2] = (-v[0]) / zz;
-    J.m[3] = 0.0f;        J.m[4] = 1.0f / v[2]; J.m[5] = (-v[1]) / zz;
-    J.m[6] = 0.0f;        J.m[7] = 0.0f;        J.m[8] = 0.0f;
-    const M3 Tm = mul3(mul3(transpose3(T), C), J);
-    return mul3(transpose3(Tm), Tm);
-}
-
-__device__ __forceinline__ float wgsl_sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
-
-__constant__ float c_shc[16] = {
-    0.28209479177387814f,  -0.4886025119029199f, 0.4886025119029199f,  -0.4886025119029199f,
-    1.0925484305920792f,   -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
-    0.5462742152960396f,   -0.5900435899266435f, 2.890611442640554f,   -0.4570457994644658f,
-    0.3731763325901154f,   -0.4570457994644658f, 1.445305721320277f,   -0.5900435899266435f,
-};
-
 template <int SHO>
 __device__ __forceinline__ void load_sh(const float* __restrict__ sh, uint32_t i, float* out) {
     constexpr int NF = 3 * (SHO + 1) * (SHO + 1);
@@ -280,36 +173,6 @@ __device__ __forceinline__ void load_sh(const float* __restrict__ sh, uint32_t i
     }
 }
 
-// sphericalHarmonicsLookup (shaders.wgsl:268-294)
-template <int SHO>
-__device__ __forceinline__ float sh_channel(const float* sh, int c, float x, float y, float z, float xx, float yy,
-                                            float zz) {
-    float col = 0.5f;
-    col = col + c_shc[0] * sh[c];
-    if (SHO > 0) {
-        col = col + (c_shc[1] * sh[3 + c]) * y;
-        col = col + (c_shc[2] * sh[6 + c]) * z;
-        col = col + (c_shc[3] * sh[9 + c]) * x;
-    }
-    if (SHO > 1) {
-        col = col + ((c_shc[4] * sh[12 + c]) * x) * y;
-        col = col + ((c_shc[5] * sh[15 + c]) * y) * z;
-        col = col + (c_shc[6] * sh[18 + c]) * ((2.0f * zz - xx) - yy);
-        col = col + ((c_shc[7] * sh[21 + c]) * x) * z;
-        col = col + (c_shc[8] * sh[24 + c]) * (xx - yy);
-    }
-    if (SHO > 2) {
-        col = col + ((c_shc[9] * sh[27 + c]) * y) * (3.0f * xx - yy);
-        col = col + (((c_shc[10] * sh[30 + c]) * x) * y) * z;
-        col = col + ((c_shc[11] * sh[33 + c]) * y) * ((4.0f * zz - xx) - yy);
-        col = col + ((c_shc[12] * sh[36 + c]) * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
-        col = col + ((c_shc[13] * sh[39 + c]) * x) * ((4.0f * zz - xx) - yy);
-        col = col + ((c_shc[14] * sh[42 + c]) * z) * (xx - yy);
-        col = col + ((c_shc[15] * sh[45 + c]) * x) * (xx - 3.0f * yy);
-    }
-    return col;
-}
-
 template <int SHO, bool COV, bool RECT>
 __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
                                                     const FrameCounters* __restrict__ fc, float4* __restrict__ rec,
@@ -322,88 +185,33 @@ __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, con
         const float4 sca = __ldg(s.scale_alpha + i);
         float sh[48];
         load_sh<SHO>(s.sh, i, sh);
-        // colour (shaders.wgsl:531-532)
-        const float vx = cx - u.camera[12], vy = cy - u.camera[13], vz = cz - u.camera[14];
-        const float len = sqrtf((vx * vx + vy * vy) + vz * vz);
-        const float dx = vx / len, dy = vy / len, dz = vz / len;
-        const float dxx = dx * dx, dyy = dy * dy, dzz = dz * dz;
-        const float cr = sh_channel<SHO>(sh, 0, dx, dy, dz, dxx, dyy, dzz);
-        const float cg = sh_channel<SHO>(sh, 1, dx, dy, dz, dxx, dyy, dzz);
-        const float cb = sh_channel<SHO>(sh, 2, dx, dy, dz, dxx, dyy, dzz);
-        // conic + decomposition (shaders.wgsl:533-542)
-        const float sx = sca.x * u.splat_scale, sy = sca.y * u.splat_scale, sz = sca.z * u.splat_scale;
-        const M3 M = projected_contour(u, sx, sy, sz, rot, cx, cy, cz);
-        const float Mxx = M.m[0], Mxy = M.m[1], Mxz = M.m[2], Myy = M.m[4], Myz = M.m[5], Mzz = M.m[8];
-        // extractTranslationOfEllipse (shaders.wgsl:179-191)
-        const float disc = Mxx * Myy - Mxy * Mxy;
-        const float inv = 1.0f / disc;
-        const float t0 = (Mxy * Myz - Myy * Mxz) * inv;
-        const float t1 = (Mxy * Mxz - Mxx * Myz) * inv;
-        // extractRotationOfEllipse (shaders.wgsl:193-215)
-        const float ra = (Mxx - Myy) * (Mxx - Myy);
-        const float rb = ra + (4.0f * Mxy) * Mxy;
-        const float rc = 0.5f * sqrtf(ra / rb);
-        float rj = sqrtf(0.5f - rc);
-        float rk = ((-sqrtf(0.5f + rc)) * wgsl_sign(Mxy)) * wgsl_sign(Mxx - Myy);
-        if (Mxy < 0.0f || Mxx - Myy < 0.0f) {
-            rk = -rk;
-            rj = -rj;
-        }
-        if (Mxx - Myy < 0.0f) {
-            const float tmp = rj;
-            rj = -rk;
-            rk = tmp;
-        }
-        float ax0, ax1;
-        if (COV) {
-            // extractScaleOfCovariance(projectedCovarianceOfEllipsoid) (shaders.wgsl:240-246, 99-118)
-            const M3 P = projected_covariance(u, sx, sy, sz, rot, cx, cy, cz);
-            const float pxx = P.m[0], pxy = P.m[1], pyy = P.m[4];
-            const float a = (pxx - pyy) * (pxx - pyy);
-            const float b = sqrtf(a + (4.0f * pxy) * pxy);
-            ax0 = sqrtf(((pxx + pyy) + b) * 0.5f);
-            ax1 = sqrtf(((pxx + pyy) - b) * 0.5f);
-        } else {
-            // extractScaleOfEllipse (shaders.wgsl:217-237)
-            const float d = ((2.0f * Mxy) * rj) * rk;
-            const float e = Mzz - (((Mxx * t0) * t0 + (Myy * t1) * t1) + ((2.0f * Mxy) * t0) * t1);
-            ax0 = sqrtf(fabsf(e / (((Mxx * rk) * rk + (Myy * rj) * rj) - d)));
-            ax1 = sqrtf(fabsf(e / (((Mxx * rj) * rj + (Myy * rk) * rk) + d)));
-        }
-        // rect basis (shaders.wgsl:543-547) and its inverse (shaders.wgsl:563-566), folded with the
-        // pixel -> view-plane mapping so that tc is affine in the pixel centre.
-        const float sa = u.bias + ax0, sb = u.bias + ax1;
-        const float Xx = rk * sa, Xy = (-rj) * sa;
-        const float Yx = rj * sb, Yy = rk * sb;
-        const float det = Xx * Yy - Xy * Yx;
-        const float idet = 1.0f / det;
-        const float i00 = Yy * idet, i01 = (-Yx) * idet, i10 = (-Xy) * idet, i11 = Xx * idet;
+        VertexOut<float> o;
+        vertex_math<SHO, COV, float>(u, cx, cy, cz, rot.x, rot.y, rot.z, rot.w, sca.x, sca.y, sca.z, sh, o);
+        // pixel box of the rectangle (or AA square) and validity
         const float vw = u.view_size[0], vh = u.view_size[1];
         const float Wf = (float)u.image_size[0], Hf = (float)u.image_size[1];
         const float psx = (2.0f * vw) / Wf, psy = -((2.0f * vh) / Hf);
-        const float bx = (-vw) - t0, by = vh - t1;
-        const float A00 = i00 * psx, A01 = i01 * psy, B0 = i00 * bx + i01 * by;
-        const float A10 = i10 * psx, A11 = i11 * psy, B1 = i10 * bx + i11 * by;
         const float m = u.margin;
         float ex, ey, R = 0.0f;
         if (RECT) {
-            ex = m * (fabsf(Xx) + fabsf(Yx));
-            ey = m * (fabsf(Xy) + fabsf(Yy));
+            ex = m * (fabsf(o.Xx) + fabsf(o.Yx));
+            ey = m * (fabsf(o.Xy) + fabsf(o.Yy));
         } else {
-            R = sqrtf(fmaxf(Xx * Xx + Xy * Xy, Yx * Yx + Yy * Yy)) * m;
+            R = sqrtf(fmaxf(o.Xx * o.Xx + o.Xy * o.Xy, o.Yx * o.Yx + o.Yy * o.Yy)) * m;
             ex = R;
             ey = R;
         }
-        const float cxp = (t0 + vw) / psx, exq = ex / psx;
-        const float cyp = (t1 - vh) / psy, eyq = ey / (-psy);
+        const float cxp = (o.t0 + vw) / psx, exq = ex / psx;
+        const float cyp = (o.t1 - vh) / psy, eyq = ey / (-psy);
         // pixels whose centre (p + 0.5) lies in the exact box, widened by 1/64 px against rounding
         const float eps = 0.015625f;
         const float fx0 = ceilf(((cxp - exq) - eps) - 0.5f), fx1 = floorf(((cxp + exq) + eps) - 0.5f);
         const float fy0 = ceilf(((cyp - eyq) - eps) - 0.5f), fy1 = floorf(((cyp + eyq) + eps) - 0.5f);
         const float al = sca.w;
-        bool ok = isfinite(A00) && isfinite(A01) && isfinite(B0) && isfinite(A10) && isfinite(A11) && isfinite(B1) &&
-                  isfinite(cr) && isfinite(cg) && isfinite(cb) && isfinite(fx0) && isfinite(fx1) && isfinite(fy0) &&
-                  isfinite(fy1) && isfinite(R) && isfinite(bx) && isfinite(by) && (al >= 1.0f / 255.0f);
+        bool ok = isfinite(o.A00) && isfinite(o.A01) && isfinite(o.B0) && isfinite(o.A10) && isfinite(o.A11) &&
+                  isfinite(o.B1) && isfinite(o.cr) && isfinite(o.cg) && isfinite(o.cb) && isfinite(fx0) &&
+                  isfinite(fx1) && isfinite(fy0) && isfinite(fy1) && isfinite(R) && isfinite(o.bx) && isfinite(o.by) &&
+                  (al >= 1.0f / 255.0f);
         uint32_t lo = 0xFFFFFFFFu, hi = 0u;
         if (ok) {
             const float cx0 = fmaxf(fx0, 0.0f), cx1 = fminf(fx1, Wf - 1.0f);
@@ -413,11 +221,11 @@ __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, con
                 hi = (uint32_t)(int)cx1 | ((uint32_t)(int)cy1 << 16);
             }
         }
-        float4* o = rec + (size_t)slot * 4;
-        o[0] = make_float4(A00, A01, B0, A10);
-        o[1] = make_float4(A11, B1, al, __uint_as_float(lo));
-        o[2] = make_float4(cr, cg, cb, __uint_as_float(hi));
-        o[3] = RECT ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : make_float4(bx, by, R, 0.0f);
+        float4* q = rec + (size_t)slot * 4;
+        q[0] = make_float4(o.A00, o.A01, o.B0, o.A10);
+        q[1] = make_float4(o.A11, o.B1, al, __uint_as_float(lo));
+        q[2] = make_float4(o.cr, o.cg, o.cb, __uint_as_float(hi));
+        q[3] = RECT ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : make_float4(o.bx, o.by, R, 0.0f);
         boxes[slot] = make_uint2(lo, hi);  // compact copy for the binning kernel
     }
 }

@@ -32,7 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "1080p frames/s @6M splats"
+METRIC = "1080p frames/s @6M splats, served vs plain loop, p50/p99 ms, PSNR\u226560dB vs ref"
 WORKLOAD = "6M splats, SH degree 3, clustered 40^3 box, 1920x1080, fovy 60, 128-pose fly-through"
 
 
@@ -48,6 +48,14 @@ def parse_args(argv=None):
     p.add_argument("--poses", type=int, default=128)
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-differentiation", action="store_true", help="skip the forward+backward leg")
+    p.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain leg")
+    p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--serve-requests", type=int, default=800, help="closed-loop requests per loop")
+    p.add_argument("--serve-rates", default="250,1000,2000", help="Poisson arrival rates (req/s)")
+    p.add_argument("--serve-seconds", type=float, default=0.5, help="arrival span per rate")
+    p.add_argument("--serve-evict-frac", type=float, default=0.5,
+                   help="scene memory budget of the eviction measurement, as a fraction of the scenes' footprint")
     p.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU-baseline sample budget")
     p.add_argument("--out", default=None, help="also write the JSON line to this file")
     return p.parse_args(argv)
@@ -62,29 +70,88 @@ def dist_info():
 
 # ---------------------------------------------------------------------------------------------------
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms while the timed region runs."""
+    """SM clock, power and clock-event reasons sampled DURING the timed region: NVML read through
+    ctypes every 5 ms on a thread (read-only queries), else nvidia-smi every 100 ms."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
-        self.gpu_index = gpu_index
+    def __init__(self, cuda_device, smi_index):
+        self.cuda_device = cuda_device
+        self.smi_index = smi_index
+        self.samples = []  # (sm_mhz, reasons mask)
+        self.max_mhz = None
+        self._stop = threading.Event()
+        self._thread = None
         self.proc = None
         self.path = None
+        self.source = None
+
+    def _nvml_handle(self):
+        import ctypes
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(self.cuda_device).uuid)
+            for cand in (uuid, "GPU-" + uuid):
+                if nv.nvmlDeviceGetHandleByUUID(cand.encode(), ctypes.byref(h)) == 0:
+                    return nv, h
+        except Exception:
+            pass
+        if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.smi_index), ctypes.byref(h)) != 0:
+            raise RuntimeError("no NVML handle")
+        return nv, h
 
     def start(self):
+        import ctypes
+        try:
+            nv, h = self._nvml_handle()
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                nv.nvmlDeviceGetCurrentClocksThrottleReasons
+
+            def loop():
+                clk, mask = ctypes.c_uint(), ctypes.c_ulonglong()
+                while not self._stop.is_set():
+                    if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and \
+                            get_reasons(h, ctypes.byref(mask)) == 0:
+                        self.samples.append((float(clk.value), int(mask.value)))
+                    self._stop.wait(0.005)
+
+            self._thread = threading.Thread(target=loop, daemon=True)
+            self._thread.start()
+            self.source = "nvml 5 ms"
+            return
+        except Exception:
+            self._thread = None
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-i", str(self.gpu_index), "-lms", "200"], stdout=open(self.path, "w"),
+                                          "-i", str(self.smi_index), "-lms", "100"], stdout=open(self.path, "w"),
                                          stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # let the first samples arrive before the timed region starts
+            self.source = "nvidia-smi 100 ms"
         except Exception:
             self.proc = None
 
     def stop(self):
+        if self._thread is not None:
+            self._stop.set()
+            self._thread.join(timeout=2)
+            sm = [c for c, _ in self.samples]
+            reasons = sorted({name for _, m in self.samples for bit, name in self.REASONS.items() if m & bit})
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz,
+                    "reasons": reasons, "samples": len(sm), "source": self.source}
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"], "samples": 0}
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -106,7 +173,7 @@ class ClockSampler:
                     reasons.add(nm)
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": self.source}
 
 
 # ---------------------------------------------------------------------------------------------------
@@ -203,7 +270,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     visible = os.environ.get("CUDA_VISIBLE_DEVICES", "")
     gpu_index = int(visible.split(",")[dev]) if visible and visible.split(",")[dev].strip().isdigit() else dev
-    clocks = ClockSampler(gpu_index)
+    clocks = ClockSampler(dev, gpu_index)
     clocks.start()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -275,6 +342,16 @@ def run_ours(args):
 
     launches = r.launches_per_frame(W, H) * args.steps
 
+    diff = None
+    if rank == 0 and world == 1 and not args.no_differentiation:
+        diff = run_differentiation(args)
+
+    serving = None
+    if rank == 0 and world == 1 and not args.no_serving:
+        del s, r, out
+        torch.cuda.empty_cache()
+        serving = run_serving(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, rec, poses, budget_s=args.cpu_budget_s)
@@ -290,7 +367,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "splats_per_s": round(value * args.splats, 0),
             "stages": stages, "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "differentiation": diff, "serving": serving,
         }
         s_line = json.dumps(line)
         print(s_line, flush=True)
@@ -300,6 +377,237 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+DIFF_WORKLOAD = ("1M splats, SH degree 3, clustered, 1024x1024, 8 orbit views; targets from the seed scene, "
+                 "forward on a copy with positions + N(0, 0.01^2), log-scales + N(0, 0.05^2), opacity logits + "
+                 "N(0, 0.2^2); L2 image loss; fp32 blend")
+
+
+def run_differentiation(args, iters=5, warmup=3):
+    """Forward+backward ms/iter through torch.autograd (render_raw: the loader's activations in torch,
+    the hand-written backward behind the autograd Function).  One iteration = the 8 views, each
+    rendered, compared with its target and back-propagated (gradients accumulate over the views)."""
+    import numpy as np
+    import torch
+    from splatter_gb300 import BlendMode, Configuration, Renderer, camera, synthetic
+    from splatter_gb300.autograd import render_raw
+
+    n, W, H, views = 1_000_000, 1024, 1024, 8
+    rec = synthetic.clustered(n, seed=args.seed + 11, sh_order=3)
+    poses = camera.orbit_poses(views, seed=args.seed + 13)
+    cfg = Configuration(max_splat_count=n, spherical_harmonics_order=3, blend_mode=BlendMode.FP32,
+                        field_of_view_y=math.radians(60.0))
+    r = Renderer(cfg)
+    dev = "cuda"
+
+    def params(a):
+        t = torch.tensor(a, device=dev)
+        return (t[:, 0:3].contiguous(), t[:, 58:62].contiguous(), t[:, 55:58].contiguous(), t[:, 54].contiguous(),
+                t[:, 6:54].contiguous())
+
+    with torch.no_grad():
+        seed_p = params(rec)
+        targets = [render_raw(*seed_p[:4], seed_p[4], r, poses[v], W, H)[..., :3].clone() for v in range(views)]
+    rng = np.random.default_rng(args.seed + 17)
+    pert = rec.copy()
+    pert[:, 0:3] += rng.normal(0.0, 0.01, (n, 3)).astype(np.float32)
+    pert[:, 55:58] += rng.normal(0.0, 0.05, (n, 3)).astype(np.float32)
+    pert[:, 54] += rng.normal(0.0, 0.2, n).astype(np.float32)
+    leaves = [t.requires_grad_(True) for t in params(pert)]
+
+    def iteration():
+        for t in leaves:
+            t.grad = None
+        total = 0.0
+        for v in range(views):
+            img = render_raw(leaves[0], leaves[1], leaves[2], leaves[3], leaves[4], r, poses[v], W, H)
+            loss = ((img[..., :3] - targets[v]) ** 2).sum()
+            loss.backward()
+            total = total + loss.detach()
+        return total
+
+    for _ in range(warmup):
+        iteration()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(iters):
+        loss = iteration()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    # forward alone (no graph), same views
+    with torch.no_grad():
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(iters):
+            for v in range(views):
+                render_raw(*[t.detach() for t in leaves[:4]], leaves[4].detach(), r, poses[v], W, H)
+        f1.record(stream)
+        torch.cuda.synchronize()
+    ms_fwd = f0.elapsed_time(f1) / iters
+    finite = all(bool(torch.isfinite(t.grad).all()) for t in leaves)
+    return {"workload": DIFF_WORKLOAD, "ms_per_iter": round(ms, 3), "ms_forward_per_iter": round(ms_fwd, 3),
+            "views": views, "splats": n, "iters": iters, "warmup": warmup, "loss": float(loss),
+            "grads_finite": finite,
+            "note": "device-timed (CUDA events around whole iterations, python/autograd overhead included)"}
+
+
+SERVE_RES = [(512, 512), (1280, 720), (1920, 1080)]
+SERVE_WORKLOAD = ("24 resident scenes of 200k-6M splats (log-uniform, clustered 40^3 box, SH 3; 8 GB, all within "
+                  "the scene memory budget); requests with uniform random scene, orbit pose (radius 6-12, fovy 60) "
+                  "and viewport from {512x512, 1280x720, 1920x1080}; RGBA8 results copied to page-locked host "
+                  "memory.  'eviction' repeats the closed loop with a budget of half the scenes' footprint (LRU "
+                  "eviction to page-locked host memory, scenes copied back on demand)")
+
+
+def _serve_requests(count, seed, n_scenes):
+    import numpy as np
+    from splatter_gb300 import camera
+    rng = np.random.default_rng(seed)
+    poses = camera.orbit_poses(count, seed=seed + 1, radius=(6.0, 12.0))
+    return [(int(rng.integers(n_scenes)), np.asarray(poses[i], np.float32), SERVE_RES[int(rng.integers(3))])
+            for i in range(count)]
+
+
+def _pct(xs, q):
+    import numpy as np
+    return round(float(np.percentile(np.asarray(xs, np.float64), q)), 3) if xs else None
+
+
+def _serve_one(server, reqs, pools, keep_first=0):
+    """Closed loop with `len(pool)` requests outstanding: saturation throughput and latencies."""
+    import torch
+    from splatter_gb300.serving import now_ns
+    pending, done, kept = {}, [], {}
+    it = iter(enumerate(reqs))
+
+    def submit_next():
+        nxt = next(it, None)
+        if nxt is None:
+            return False
+        i, (sid, pose, (w, h)) = nxt
+        buf = pools[(w, h)].pop()
+        tag = server.submit(sid, pose, w, h, buf, tag=i + 1)
+        pending[tag] = ((w, h), buf, i)
+        return True
+
+    t0 = now_ns()
+    q = min(len(p) for p in pools.values())
+    while len(pending) < q and submit_next():
+        pass
+    while pending:
+        for c in server.poll(timeout_us=200000):
+            res, buf, i = pending.pop(c.tag)
+            if c.status != 0:
+                raise RuntimeError(f"request {i} failed with status {c.status}")
+            if i < keep_first:
+                kept[i] = buf.clone()
+            pools[res].append(buf)
+            done.append(c)
+            submit_next()
+    t1 = max(c.t_done_ns for c in done)
+    lat = [(c.t_done_ns - c.t_submit_ns) / 1e6 for c in done]
+    return {"frames_per_s": round(len(done) / ((t1 - t0) / 1e9), 1), "p50_ms": _pct(lat, 50),
+            "p99_ms": _pct(lat, 99), "requests": len(done)}, kept
+
+
+def _serve_poisson(server, reqs, pools, rate, seed):
+    """Open loop: Poisson arrivals at `rate` req/s; latency from the intended arrival time (so a
+    backlog, including waits for a free result buffer, counts)."""
+    import numpy as np
+    from splatter_gb300.serving import now_ns
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(reqs))
+    t_start = now_ns() + 2_000_000
+    arrivals = t_start + np.cumsum(gaps * 1e9).astype(np.int64)
+    pending, lat, t_last = {}, [], 0
+
+    def reap(timeout_us):
+        nonlocal t_last
+        for c in server.poll(timeout_us=timeout_us):
+            res, buf, arr = pending.pop(c.tag)
+            if c.status != 0:
+                raise RuntimeError(f"request failed with status {c.status}")
+            pools[res].append(buf)
+            lat.append((c.t_done_ns - arr) / 1e6)
+            t_last = max(t_last, c.t_done_ns)
+
+    for i, ((sid, pose, (w, h)), arr) in enumerate(zip(reqs, arrivals)):
+        while True:
+            reap(0)
+            wait = (int(arr) - now_ns()) / 1e9
+            if wait <= 0:
+                break
+            time.sleep(min(wait, 0.0005))
+        while not pools[(w, h)]:
+            reap(100000)
+        buf = pools[(w, h)].pop()
+        tag = server.submit(sid, pose, w, h, buf, tag=i + 1)
+        pending[tag] = ((w, h), buf, int(arr))
+    while pending:
+        reap(200000)
+    span = (t_last - int(arrivals[0])) / 1e9
+    return {"rate": rate, "achieved_per_s": round(len(lat) / span, 1), "p50_ms": _pct(lat, 50),
+            "p99_ms": _pct(lat, 99), "requests": len(lat)}
+
+
+def run_serving(args):
+    """Served loop (slots x frames in flight, captured frame graphs) against the plain loop (one
+    request at a time, direct launches) over the same scenes and requests."""
+    import torch
+    from splatter_gb300 import Configuration, DepthSorting, BlendMode, synthetic
+    from splatter_gb300.serving import Server
+    sizes = synthetic.serving_scene_sizes(24)
+    footprint = sum((n * 236 + 255) // 256 * 256 for n in sizes)
+    cfg = Configuration(depth_sorting=DepthSorting.GPU, use_covariance_for_scale=True, use_unaligned_rectangles=True,
+                        spherical_harmonics_order=3, max_splat_count=max(sizes),
+                        field_of_view_y=math.radians(60.0), blend_mode=BlendMode.UNORM8)
+    warm = _serve_requests(args.serve_requests // 2, seed=args.seed + 31, n_scenes=len(sizes))
+    closed = _serve_requests(args.serve_requests, seed=args.seed + 37, n_scenes=len(sizes))
+    rates = [float(x) for x in args.serve_rates.split(",") if x]
+    out = {"workload": SERVE_WORKLOAD, "scenes": len(sizes), "scene_splats": sizes,
+           "scene_bytes_total": footprint}
+    kept = {}
+    evict_budget = int(args.serve_evict_frac * footprint)
+    out["eviction_budget"] = evict_budget
+    for name, slots, graphs in (("plain", 1, False), ("served", args.serve_slots, True)):
+        res = None
+        for budget_now in (0, evict_budget):
+            srv = Server(cfg, slots=slots, use_graphs=graphs, scene_memory_budget=budget_now, max_width=1920,
+                         max_height=1080)
+            for i, n in enumerate(sizes):
+                rec = synthetic.clustered_device(n, seed=1000 + i)
+                srv.add_scene(rec)
+                del rec
+            torch.cuda.synchronize()
+            depth = max(2, 2 * slots)
+            pools = {r: [srv.output_buffer(*r) for _ in range(max(depth, 48))] for r in SERVE_RES}
+            _serve_one(srv, warm, {r: p[:depth] for r, p in pools.items()})
+            if budget_now == 0:
+                res, kept[name] = _serve_one(srv, closed, {r: p[:depth] for r, p in pools.items()}, keep_first=16)
+                res["rates"] = [_serve_poisson(srv, _serve_requests(max(100, int(rate * args.serve_seconds)),
+                                                                    seed=args.seed + 41 + k, n_scenes=len(sizes)),
+                                               pools, rate, seed=args.seed + 43 + k) for k, rate in enumerate(rates)]
+                st = srv.stats()
+                res.update({"slots": slots, "graphs": graphs, "outstanding": depth,
+                            "graphs_captured": st["graphs_captured"], "max_in_flight": st["max_in_flight"]})
+            else:
+                st0 = srv.stats()
+                ev, _ = _serve_one(srv, closed, {r: p[:depth] for r, p in pools.items()})
+                st = srv.stats()
+                ev.update({"evictions": st["evictions"] - st0["evictions"], "restores": st["restores"] - st0["restores"]})
+                res["eviction"] = ev
+            srv.close()
+            del pools
+        out[name] = res
+    same = all(torch.equal(kept["plain"][i], kept["served"][i]) for i in kept["plain"])
+    out["throughput_ratio"] = round(out["served"]["frames_per_s"] / out["plain"]["frames_per_s"], 2)
+    out["results_identical_to_plain"] = bool(same)
+    out["psnr_vs_plain_db"] = "inf" if same else None
+    return out
 
 
 def cpu_baseline(args, rec, poses, budget_s=20.0, threads=None):

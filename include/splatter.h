@@ -232,6 +232,83 @@ SPL_API int spl_renderer_stage_times(spl_renderer* r, float* milliseconds, int c
  * viewport. */
 SPL_API int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint32_t height);
 
+/* ---- sort algorithm (extension) -----------------------------------------------------------------
+ * COOPERATIVE (default): each sort (the 4 depth passes, the <= 3 tile-id passes) is one cooperative
+ * launch with grid-wide barriers; it assumes the whole device, so only one such frame may run at a
+ * time.  ONESWEEP: one launch per pass with decoupled look-back over dynamically numbered tiles,
+ * safe when several renderers run frames concurrently on different streams (the serving runtime
+ * uses it).  Both are stable and give identical results. */
+#define SPL_SORT_COOPERATIVE 0
+#define SPL_SORT_ONESWEEP 1
+SPL_API int spl_renderer_set_sort_mode(spl_renderer* r, int mode);
+
+/* ---- captured frames (extension) ----------------------------------------------------------------
+ * A frame at width x height into `out_device`, captured once into a CUDA graph with grids sized for
+ * the renderer's max_splat_count; each launch replays it for any scene and camera (only the first
+ * kernel's parameters change: the kernels read the scene and every count from device memory), on
+ * any stream.  The renderer's scratch is shared with its other frames: one frame of a renderer in
+ * flight at a time.  Destroy the graph before the renderer or the output buffer. */
+typedef struct spl_frame_graph spl_frame_graph;
+SPL_API int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, void* out_device,
+                                   spl_frame_graph** out);
+SPL_API int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16],
+                                   void* stream);
+SPL_API void spl_frame_graph_destroy(spl_frame_graph* g);
+
+/* Scene::load_chunk from 62-float records already in device memory (no staging). */
+SPL_API int spl_scene_load_chunk_device(spl_scene* s, const float* records_device, uint64_t start, uint64_t count,
+                                        void* stream);
+
+/* ---- serving runtime (extension; no reference counterpart) --------------------------------------
+ * Many scenes resident on the device, admitted by their device footprint against a budget; scenes
+ * beyond it are evicted least-recently-used (their page-locked host copies stay and are copied back
+ * on the next request).  Requests of any scene, pose and viewport are admitted continuously as
+ * slots free up: each slot owns a renderer's scratch, a stream and an output buffer, so the frames
+ * of different slots overlap on the device; with use_graphs each slot replays a captured frame
+ * graph per viewport.  One scheduler thread per server issues all device work. */
+typedef struct spl_server spl_server;
+typedef struct spl_server_config {
+    uint32_t slots;               /* frames in flight (>= 1) */
+    uint32_t use_graphs;          /* 1: replay captured frame graphs; 0: launch each frame's kernels */
+    uint64_t scene_memory_budget; /* device bytes for resident scenes; 0 = no limit */
+    uint32_t max_width;           /* largest viewport a request may ask for */
+    uint32_t max_height;
+} spl_server_config;
+typedef struct spl_request {
+    uint64_t tag;                 /* returned in the completion */
+    uint32_t scene_id;
+    uint32_t width, height;
+    float camera_to_world[16];
+    void* host_out;               /* width*height*4 bytes (UNORM8) or *16 (FP32); page-locked lets it overlap */
+} spl_request;
+typedef struct spl_completion {
+    uint64_t tag;
+    int32_t status;               /* SPL_OK or an SPL_ERR_* code */
+    uint32_t slot;
+    uint64_t t_submit_ns, t_start_ns, t_done_ns; /* spl_server_now_ns clock */
+    uint32_t restored;            /* 1 when this request copied its scene back to the device */
+    uint32_t reserved;
+} spl_completion;
+typedef struct spl_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t resident_scenes, resident_bytes, evictions, restores;
+    uint64_t graphs_captured, graph_launches, direct_launches, max_in_flight;
+} spl_server_stats;
+SPL_API int spl_server_create(const spl_config* cfg, const spl_server_config* scfg, spl_server** out);
+/* Waits for the requests in flight, then frees everything. */
+SPL_API void spl_server_destroy(spl_server* s);
+/* Adds a scene from `count` 62-float file records (host memory, or device memory when
+ * records_on_device != 0); returns its id. */
+SPL_API int spl_server_add_scene(spl_server* s, const float* records62, uint64_t count, int records_on_device,
+                                 uint32_t* scene_id);
+/* Queues a request (thread-safe, does not block on the device). */
+SPL_API int spl_server_submit(spl_server* s, const spl_request* req);
+/* Up to `capacity` completions; waits up to timeout_us (< 0: forever) for the first one. */
+SPL_API int spl_server_poll(spl_server* s, spl_completion* out, uint32_t capacity, uint32_t* count,
+                            int64_t timeout_us);
+SPL_API int spl_server_get_stats(spl_server* s, spl_server_stats* out);
+SPL_API uint64_t spl_server_now_ns(void);
+
 SPL_API const char* spl_last_error_string(void);
 /* Runs one bounded look-back wait against a predecessor that never publishes, with a wait limit of
  * `spin_limit` polls, and reports whether the kernel returned with the timeout flag set

@@ -1075,6 +1075,42 @@ OAPI void* oracle_grad_create(const void* uni, const void* cfgp, uint64_t n, con
 
 OAPI void oracle_grad_destroy(void* h) { delete (GradCtx*)h; }
 
+namespace {
+void rebuild_tiles(GradCtx& g) {
+    g.tiles.assign((size_t)g.TX * g.TY, {});
+    for (size_t p = 0; p < g.rec.size(); ++p) {
+        const GRec& r = g.rec[p];
+        if (!r.valid || r.x0 > r.x1) continue;
+        for (int ty = r.y0 / 16; ty <= r.y1 / 16; ++ty)
+            for (int tx = r.x0 / 16; tx <= r.x1 / 16; ++tx) g.tiles[(size_t)ty * g.TX + tx].push_back((uint32_t)p);
+    }
+}
+}  // namespace
+
+// Replaces the screen-space records of the given splats by FP32 records in the renderer's 16-float
+// layout (A00 A01 B0 A10 | A11 B1 opacity box_lo | r g b box_hi | bx by R 0), e.g. the ones a
+// renderer produced: compositing and its gradient then run in FP64 on exactly those records, while
+// the vertex-stage Jacobian stays the FP64 one at the splat's parameters.  Isolates the compositing
+// backward from the precision of the FP32 vertex stage.
+OAPI void oracle_grad_pin_records(void* h, const float* recs16, const uint32_t* splat_idx, uint64_t count) {
+    GradCtx& g = *(GradCtx*)h;
+    for (uint64_t i = 0; i < count; ++i) {
+        const uint32_t k = splat_idx[i];
+        if (k >= g.n || g.pos_of[k] < 0) continue;
+        const float* rc = recs16 + 16 * i;
+        GRec& r = g.rec[(size_t)g.pos_of[k]];
+        r.A00 = rc[0]; r.A01 = rc[1]; r.B0 = rc[2]; r.A10 = rc[3];
+        r.A11 = rc[4]; r.B1 = rc[5]; r.a = rc[6];
+        r.rgb[0] = rc[8]; r.rgb[1] = rc[9]; r.rgb[2] = rc[10];
+        r.bx = rc[12]; r.by = rc[13]; r.R = rc[14];
+        const uint32_t lo = float_to_bits(rc[7]), hi = float_to_bits(rc[11]);
+        r.x0 = (int)(lo & 0xFFFFu); r.y0 = (int)(lo >> 16); r.x1 = (int)(hi & 0xFFFFu); r.y1 = (int)(hi >> 16);
+        r.valid = r.x0 <= r.x1 && r.y0 <= r.y1;
+        if (!r.valid) { r.x0 = 1; r.x1 = 0; r.y0 = 1; r.y1 = 0; }
+    }
+    rebuild_tiles(g);
+}
+
 // Full-frame FP64 loss; grads (n x 59) receive the analytic FP64 gradient (zero for splats not drawn).
 OAPI double oracle_grad_loss_ex(void* h, double* grads, double* image_out, int threads, double* rec_grads_out,
                                 uint32_t* order_out);

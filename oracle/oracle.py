@@ -218,6 +218,8 @@ class GradContext:
             L.oracle_grad_loss.argtypes = [P, P, P, ctypes.c_int]
             L.oracle_grad_fd.restype = ctypes.c_int
             L.oracle_grad_fd.argtypes = [P, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, P]
+            L.oracle_grad_pin_records.restype = None
+            L.oracle_grad_pin_records.argtypes = [P, P, P, ctypes.c_uint64]
             L.oracle_grad_jacobian.restype = None
             L.oracle_grad_jacobian.argtypes = [P, ctypes.c_uint64, P]
             L.oracle_grad_loss_ex.restype = ctypes.c_double
@@ -246,6 +248,15 @@ class GradContext:
         order = np.zeros(nd, np.uint32)
         lib().oracle_grad_loss_ex(self._h, None, None, int(threads), _p(rg), _p(order))
         return rg, order
+
+    def pin_records(self, records16, splat_idx):
+        """Composite (and differentiate the compositing) in FP64 on these FP32 records (16 floats per
+        splat, renderer layout) instead of the oracle's own FP64 records; the vertex-stage Jacobian
+        stays the FP64 one."""
+        rec = np.ascontiguousarray(records16, np.float32).reshape(-1, 16)
+        idx = np.ascontiguousarray(splat_idx, np.uint32)
+        assert rec.shape[0] == idx.shape[0]
+        lib().oracle_grad_pin_records(self._h, _p(rec), _p(idx), rec.shape[0])
 
     def jacobian(self, k):
         """(10, 9) FP64 Jacobian of splat k's record (A00, A01, B0, A10, A11, B1, r, g, b; A against

@@ -3,8 +3,8 @@
 The compute path is libsplatter_cuda.so (hand-written CUDA behind the C ABI in include/splatter.h);
 this package is its Python host mirror of the reference's Renderer/Scene API.
 """
-from .renderer import (BlendMode, Configuration, DepthSorting, FrameInfo, Renderer, Scene, SplatterError,
-                       compute_uniforms)
+from .renderer import (SORT_COOPERATIVE, SORT_ONESWEEP, BlendMode, Configuration, DepthSorting, FrameGraph,
+                       FrameInfo, Renderer, Scene, SplatterError, compute_uniforms)
 
-__all__ = ["BlendMode", "Configuration", "DepthSorting", "FrameInfo", "Renderer", "Scene", "SplatterError",
-           "compute_uniforms"]
+__all__ = ["BlendMode", "Configuration", "DepthSorting", "FrameGraph", "FrameInfo", "Renderer", "Scene",
+           "SplatterError", "compute_uniforms", "SORT_COOPERATIVE", "SORT_ONESWEEP"]

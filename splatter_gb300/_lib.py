@@ -54,6 +54,49 @@ class SplFrameInfo(ctypes.Structure):
     ]
 
 
+class SplServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("slots", ctypes.c_uint32),
+        ("use_graphs", ctypes.c_uint32),
+        ("scene_memory_budget", ctypes.c_uint64),
+        ("max_width", ctypes.c_uint32),
+        ("max_height", ctypes.c_uint32),
+    ]
+
+
+class SplRequest(ctypes.Structure):
+    _fields_ = [
+        ("tag", ctypes.c_uint64),
+        ("scene_id", ctypes.c_uint32),
+        ("width", ctypes.c_uint32),
+        ("height", ctypes.c_uint32),
+        ("camera_to_world", ctypes.c_float * 16),
+        ("host_out", ctypes.c_void_p),
+    ]
+
+
+class SplCompletion(ctypes.Structure):
+    _fields_ = [
+        ("tag", ctypes.c_uint64),
+        ("status", ctypes.c_int32),
+        ("slot", ctypes.c_uint32),
+        ("t_submit_ns", ctypes.c_uint64),
+        ("t_start_ns", ctypes.c_uint64),
+        ("t_done_ns", ctypes.c_uint64),
+        ("restored", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+    ]
+
+
+class SplServerStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint64) for name in (
+        "submitted", "completed", "failed", "resident_scenes", "resident_bytes", "evictions", "restores",
+        "graphs_captured", "graph_launches", "direct_launches", "max_in_flight")]
+
+
+SORT_COOPERATIVE = 0
+SORT_ONESWEEP = 1
+
 # (name, restype, argtypes) for every entry point of include/splatter.h
 P = ctypes.c_void_p
 U32 = ctypes.c_uint32
@@ -90,6 +133,18 @@ SIGNATURES = [
     ("spl_scene_wrap", I32, [P, U64, P, P, P, P, P, P, ctypes.POINTER(P)]),
     ("spl_render_backward", I32, [P, P, P, P, P, P, P, P, P, P, P]),
     ("spl_renderer_copy_record_gradients", I32, [P, P, U64, P]),
+    ("spl_renderer_set_sort_mode", I32, [P, I32]),
+    ("spl_frame_graph_create", I32, [P, U32, U32, P, ctypes.POINTER(P)]),
+    ("spl_frame_graph_launch", I32, [P, P, P, P]),
+    ("spl_frame_graph_destroy", None, [P]),
+    ("spl_scene_load_chunk_device", I32, [P, P, U64, U64, P]),
+    ("spl_server_create", I32, [CFG_P, ctypes.POINTER(SplServerConfig), ctypes.POINTER(P)]),
+    ("spl_server_destroy", None, [P]),
+    ("spl_server_add_scene", I32, [P, P, U64, I32, ctypes.POINTER(U32)]),
+    ("spl_server_submit", I32, [P, ctypes.POINTER(SplRequest)]),
+    ("spl_server_poll", I32, [P, ctypes.POINTER(SplCompletion), U32, ctypes.POINTER(U32), ctypes.c_int64]),
+    ("spl_server_get_stats", I32, [P, ctypes.POINTER(SplServerStats)]),
+    ("spl_server_now_ns", U64, []),
 ]
 
 NO_ALLOC_MAX_PAIRS = 262144

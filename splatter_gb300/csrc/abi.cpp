@@ -13,77 +13,42 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/splatter.h"
-#include "spl_types.h"
+#include "spl_internal.h"
 
 using namespace spl;
 
 namespace {
-
 thread_local std::string g_err;
-
-int fail(int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
-    g_err = buf;
-    return code;
-}
-
-#define CU(call)                                                                                     \
-    do {                                                                                             \
-        cudaError_t e_ = (call);                                                                     \
-        if (e_ != cudaSuccess) return fail(SPL_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                                           __FILE__, __LINE__);                                      \
-    } while (0)
-
-constexpr uint64_t MAX_COUNT = (1ull << 30) - 1;  // look-back status words carry 30-bit counts
-constexpr uint32_t DEFAULT_SPIN_LIMIT = 1u << 20;
-constexpr uint64_t CHUNK_RECORDS = 1u << 16;  // staging ring piece (16.25 MB of 248-byte records)
-
-template <typename T>
-int dalloc(T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) return SPL_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        *p = nullptr;
-        return fail(SPL_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
-    }
-    return SPL_OK;
-}
-
-template <typename T>
-void dfree(T*& p) {
-    if (p) cudaFree(p);
-    p = nullptr;
-}
-
-uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
-
 }  // namespace
 
-// Error reporting for the other translation units of the library.
-int spl_internal_fail(int code, const char* fmt, ...) {
+namespace spl {
+int vfail(int code, const char* fmt, va_list ap) {
     char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
     vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
     g_err = buf;
     return code;
 }
+}  // namespace spl
+
+int spl_internal_fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    const int rc = spl::vfail(code, fmt, ap);
+    va_end(ap);
+    return rc;
+}
+
 
 // Frame uniforms (renderer.rs:364-409; utils.rs:45-70).  The camera is the camera-to-world matrix
 // (motor3d_to_mat4 of the motor, utils.rs:31-42); the view matrix is its rigid inverse (the
 // reference inverts the motor, renderer.rs:365).  field_of_view_y is a documented extension (the
 // reference fixes pi/2, renderer.rs:366); view_width = aspect * view_height equals the reference's
 // aspect / view_height there, because view_height == 1.
-static void compute_uniforms(const spl_config& cfg, const float* cam, uint32_t W, uint32_t H, Uniforms& u) {
+void spl::compute_uniforms(const spl_config& cfg, const float* cam, uint32_t W, uint32_t H, Uniforms& u) {
     std::memcpy(u.camera, cam, 64);
     for (int c = 0; c < 3; ++c)
         for (int r = 0; r < 3; ++r) u.view[c * 4 + r] = cam[r * 4 + c];
@@ -117,88 +82,6 @@ static void compute_uniforms(const spl_config& cfg, const float* cam, uint32_t W
     u.splat_scale = cfg.splat_scale;
 }
 
-struct spl_renderer {
-    spl_config cfg{};
-    int device = 0;
-    uint64_t max_n = 0;
-    uint64_t pair_cap = 0;
-    uint32_t spin_limit = DEFAULT_SPIN_LIMIT;
-    // depth sort: K1 writes keys_a/idx; 4 passes a->b->a->b->a leave (key, slot) in keys_a/vals_a
-    uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr, *idx = nullptr;
-    float4* rec = nullptr;
-    uint2* boxes = nullptr;  // pixel box of each record, for the binning kernel
-    uint64_t* st_cull = nullptr;  // [ceil(max_n/4096)]
-    uint64_t* st_bin = nullptr;   // [ceil(max_n/1024)]
-    uint32_t *pk_a = nullptr, *pk_b = nullptr, *pv_a = nullptr, *pv_b = nullptr;
-    FrameCounters* fc = nullptr;
-    FrameCounters* fc_sort = nullptr;  // counters of spl_sort_pairs
-    uint32_t* coop_cnt = nullptr;      // [256][grid, padded to 4] digit counts + [256] totals (cooperative sort)
-    uint32_t* epoch = nullptr;
-    FrameCounters* host_fc = nullptr;  // pinned
-    uint2* ranges = nullptr;
-    uint64_t ranges_cap = 0;
-    // last frame
-    cudaStream_t last_stream = nullptr;
-    bool has_frame = false;
-    uint32_t last_w = 0, last_h = 0;
-    uint64_t last_n = 0;
-    const uint32_t* final_pair_vals = nullptr;
-    const spl_scene* last_scene = nullptr;
-    Uniforms last_u{};
-    float* grad_rec = nullptr;  // [max_n][10] record gradients of the backward pass (allocated on first use)
-    // stage profiling: events 0..7 on the frame's stream
-    bool profiling = false;
-    cudaEvent_t ev_prof[8] = {};
-
-
-    void release() {
-        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes); dfree(grad_rec);
-        dfree(st_cull); dfree(st_bin);
-        dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b);
-        dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges);
-        if (host_fc) cudaFreeHost(host_fc);
-        host_fc = nullptr;
-        for (auto& e : ev_prof) {
-            if (e) cudaEventDestroy(e);
-            e = nullptr;
-        }
-    }
-    void mark(int i, cudaStream_t s) {
-        if (profiling) cudaEventRecord(ev_prof[i], s);
-    }
-};
-
-struct Staging {
-    float* pinned[2] = {nullptr, nullptr};
-    float* dev[2] = {nullptr, nullptr};
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    int next = 0;
-};
-
-struct spl_scene {
-    spl_renderer* renderer = nullptr;
-    int device = 0;
-    uint64_t n = 0;
-    bool owns = true;  // false for scenes wrapping caller-owned arrays (spl_scene_wrap)
-    float *x = nullptr, *y = nullptr, *z = nullptr, *sh = nullptr;
-    float4 *rot = nullptr, *scale_alpha = nullptr;
-    Staging stg;
-    std::mutex stg_mu;
-
-    SceneView view() const { return SceneView{x, y, z, rot, scale_alpha, sh, (uint32_t)n}; }
-    void release() {
-        if (owns) {
-            dfree(x); dfree(y); dfree(z); dfree(sh); dfree(rot); dfree(scale_alpha);
-        }
-        for (int i = 0; i < 2; ++i) {
-            if (stg.pinned[i]) cudaFreeHost(stg.pinned[i]);
-            dfree(stg.dev[i]);
-            if (stg.ev[i]) cudaEventDestroy(stg.ev[i]);
-            stg.pinned[i] = nullptr;
-            stg.ev[i] = nullptr;
-        }
-    }
-};
 
 static int validate_config(const spl_config* c) {
     if (!c) return fail(SPL_ERR_INVALID, "config is NULL");
@@ -354,6 +237,8 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
     TRY(dalloc(&r->fc, 1));
     TRY(dalloc(&r->fc_sort, 1));
     TRY(dalloc(&r->epoch, 1));
+    TRY(dalloc(&r->d_u, 1));
+    TRY(dalloc(&r->d_sv, 1));
     TRY(dalloc(&r->coop_cnt, 256 * (((size_t)sort_coop_grid() + 3) & ~(size_t)3) + 256));
 #undef TRY
     cudaError_t e = cudaSuccess;
@@ -392,13 +277,11 @@ int spl_renderer_reserve(spl_renderer* r, uint32_t width, uint32_t height) {
     return ensure_ranges(r, tiles);
 }
 
-int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
-                     uint32_t height, void* out_device, void* stream) {
-    if (!r || !scene || !camera_to_world || !out_device) return fail(SPL_ERR_INVALID, "NULL argument");
-    if (width == 0 || height == 0 || width > 65535 || height > 65535)
-        return fail(SPL_ERR_INVALID, "viewport %ux%u outside [1, 65535]", width, height);
-    if (scene->n > r->max_n) return fail(SPL_ERR_INVALID, "scene larger than the renderer's max_splat_count");
-    cudaStream_t st = (cudaStream_t)stream;
+// One frame on `st`.  grid_n sizes the grids (the scene's count, or the renderer's maximum for a
+// captured frame whose scene changes between launches: the kernels read the scene and every count
+// from device memory).
+static int render_frame_impl(spl_renderer* r, const SceneView& sv, const Uniforms& u, uint32_t width, uint32_t height,
+                             void* out_device, cudaStream_t st, uint32_t grid_n) {
     const spl_config& cfg = r->cfg;
     const uint64_t tiles_x = ceil_div(width, TILE_PIXELS), tiles_y = ceil_div(height, TILE_PIXELS);
     const uint64_t tiles = tiles_x * tiles_y;
@@ -409,26 +292,41 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
         int rc = ensure_ranges(r, tiles);
         if (rc) return rc;
     }
-    Uniforms u;
-    compute_uniforms(cfg, camera_to_world, width, height, u);
-    const SceneView sv = scene->view();
-    const uint32_t N = (uint32_t)scene->n;
+    const uint32_t N = grid_n;
     const int mode = cfg.depth_sorting;
     const uint32_t sl = r->spin_limit;
 
+    const bool coop = r->sort_mode == SPL_SORT_COOPERATIVE;
     r->mark(0, st);
-    launch_frame_begin(r->fc, r->epoch, st);
-    launch_cull_key(mode, sv, u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
+    launch_frame_begin(r->fc, r->epoch, u, r->d_u, sv, r->d_sv, st);
+    launch_cull_key(mode, N, r->d_sv, r->d_u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
     r->mark(1, st);
     launch_preprocess((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
-                      cfg.use_unaligned_rectangles != 0, sv, u, r->idx, r->fc, r->rec, r->boxes, N, st);
+                      cfg.use_unaligned_rectangles != 0, r->d_sv, r->d_u, r->idx, r->fc, r->rec, r->boxes, N, st);
     r->mark(2, st);
     const uint32_t* order = nullptr;
     if (mode != DS_NONE && N > 0) {
-        // four stable 8-bit passes a -> b -> a -> b -> a in one cooperative launch; pass 0 takes the
-        // compaction slot as the value
-        CU(launch_sort_coop(r->keys_a, r->keys_b, r->vals_a, r->vals_b, true, &r->fc->visible, N, 4, 0, r->coop_cnt,
-                            r->fc->barrier, sl, &r->fc->err, st));
+        // four stable 8-bit passes a -> b -> a -> b -> a; pass 0 takes the compaction slot as the value
+        if (coop) {
+            CU(launch_sort_coop(r->keys_a, r->keys_b, r->vals_a, r->vals_b, true, &r->fc->visible, N, 4, 0,
+                                r->coop_cnt, r->fc->barrier, sl, &r->fc->err, st));
+        } else {
+            // digit histograms from the cull kernel; one launch per pass
+            uint32_t *src_k = r->keys_a, *dst_k = r->keys_b, *dst_v = r->vals_b;
+            const uint32_t* src_v = nullptr;
+            const uint64_t stride = r->sort_tiles() * 256;
+            for (int p = 0; p < 4; ++p) {
+                launch_onesweep(src_k, src_v, dst_k, dst_v, &r->fc->visible, N, r->fc->hist_depth[p],
+                                r->st_sort + p * stride, &r->fc->tile_counter[1 + p], r->epoch, 8 * p, sl,
+                                &r->fc->err, st);
+                uint32_t* next_k = dst_k == r->keys_b ? r->keys_a : r->keys_b;
+                uint32_t* next_v = dst_v == r->vals_b ? r->vals_a : r->vals_b;
+                src_k = dst_k;
+                src_v = dst_v;
+                dst_k = next_k;
+                dst_v = next_v;
+            }
+        }
         order = r->vals_a;  // keys in keys_a
     }
     r->mark(3, st);
@@ -438,8 +336,21 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     r->mark(4, st);
     // stable sort of the pairs by tile id keeps each tile's list in depth order
     const int passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
-    CU(launch_sort_coop(r->pk_a, r->pk_b, r->pv_a, r->pv_b, false, &r->fc->pairs, (uint32_t)r->pair_cap, passes, 0,
-                        r->coop_cnt, r->fc->barrier, sl, &r->fc->err, st));
+    if (coop) {
+        CU(launch_sort_coop(r->pk_a, r->pk_b, r->pv_a, r->pv_b, false, &r->fc->pairs, (uint32_t)r->pair_cap, passes,
+                            0, r->coop_cnt, r->fc->barrier, sl, &r->fc->err, st));
+    } else {
+        // tile-id histograms from the binning kernel
+        uint32_t *ak = r->pk_a, *av = r->pv_a, *bk = r->pk_b, *bv = r->pv_b;
+        const uint64_t pstride = r->pair_tiles() * 256;
+        for (int p = 0; p < passes; ++p) {
+            launch_onesweep(ak, av, bk, bv, &r->fc->pairs, (uint32_t)r->pair_cap, r->fc->hist_pairs[p],
+                            r->st_pairs + p * pstride, &r->fc->tile_counter[5 + p], r->epoch, 8 * p, sl, &r->fc->err,
+                            st);
+            std::swap(ak, bk);
+            std::swap(av, bv);
+        }
+    }
     const uint32_t* pk = (passes & 1) ? r->pk_b : r->pk_a;
     const uint32_t* pv = (passes & 1) ? r->pv_b : r->pv_a;
     r->mark(5, st);
@@ -448,14 +359,50 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     launch_raster(cfg.use_unaligned_rectangles != 0, cfg.blend_mode, r->ranges, pv, r->rec, u, out_device, st);
     r->mark(7, st);
     CU(cudaGetLastError());
+    r->final_pair_vals = pv;
+    return SPL_OK;
+}
+
+int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
+                     uint32_t height, void* out_device, void* stream) {
+    if (!r || !scene || !camera_to_world || !out_device) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (width == 0 || height == 0 || width > 65535 || height > 65535)
+        return fail(SPL_ERR_INVALID, "viewport %ux%u outside [1, 65535]", width, height);
+    if (scene->n > r->max_n) return fail(SPL_ERR_INVALID, "scene larger than the renderer's max_splat_count");
+    cudaStream_t st = (cudaStream_t)stream;
+    Uniforms u;
+    compute_uniforms(r->cfg, camera_to_world, width, height, u);
+    const int rc = render_frame_impl(r, scene->view(), u, width, height, out_device, st, (uint32_t)scene->n);
+    if (rc) return rc;
     r->last_stream = st;
     r->last_scene = scene;
     r->last_u = u;
     r->has_frame = true;
     r->last_w = width;
     r->last_h = height;
-    r->last_n = N;
-    r->final_pair_vals = pv;
+    r->last_n = scene->n;
+    return SPL_OK;
+}
+
+int spl_renderer_set_sort_mode(spl_renderer* r, int mode) {
+    if (!r) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (mode != SPL_SORT_COOPERATIVE && mode != SPL_SORT_ONESWEEP) return fail(SPL_ERR_INVALID, "sort mode %d", mode);
+    if (mode == SPL_SORT_ONESWEEP && !r->st_sort) {
+        const uint64_t ns = r->sort_tiles() * 256 * 4, np = r->pair_tiles() * 256 * 3;
+        int rc = dalloc(&r->st_sort, ns);
+        if (rc) return rc;
+        rc = dalloc(&r->st_pairs, np);
+        if (rc) {
+            dfree(r->st_sort);
+            return rc;
+        }
+        // status words start at epoch 0, which no frame uses
+        CU(cudaMemset(r->st_sort, 0, ns * 8));
+        CU(cudaMemset(r->st_pairs, 0, np * 8));
+        CU(cudaDeviceSynchronize());
+        onesweep_prepare();
+    }
+    r->sort_mode = mode;
     return SPL_OK;
 }
 
@@ -488,11 +435,12 @@ int spl_renderer_stage_times(spl_renderer* r, float* ms, int count) {
 int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint32_t height) {
     if (!r) return 0;
     const uint64_t tiles = ceil_div(width, TILE_PIXELS) * ceil_div(height, TILE_PIXELS);
-    (void)tiles;
-    const int depth_sort = r->cfg.depth_sorting == DS_NONE ? 0 : 1;
-    // frame_begin, cull, preprocess, depth sort (one cooperative launch), ranges memset, bin,
-    // pair sort (one cooperative launch), ranges, raster
-    return 1 + 1 + 1 + depth_sort + 1 + 1 + 1 + 1 + 1;
+    const int pair_passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
+    const bool coop = r->sort_mode == SPL_SORT_COOPERATIVE;
+    const int depth_sort = r->cfg.depth_sorting == DS_NONE ? 0 : (coop ? 1 : 4);
+    // frame_begin, cull, preprocess, depth sort (one cooperative launch or 4 onesweep passes),
+    // ranges memset, bin, pair sort (one cooperative launch or one launch per pass), ranges, raster
+    return 1 + 1 + 1 + depth_sort + 1 + 1 + (coop ? 1 : pair_passes) + 1 + 1;
 }
 
 int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
@@ -832,6 +780,133 @@ int spl_parse_file_header(const char* path, uint32_t* header_bytes, uint64_t* sp
     if (pos > 0xFFFFFFFFull) return fail(SPL_ERR_IO, "header too long in %s", path);
     *header_bytes = (uint32_t)pos;
     *splat_count = count;
+    return SPL_OK;
+}
+
+// ---- captured frames ----------------------------------------------------------------------------
+struct spl_frame_graph {
+    spl_renderer* r = nullptr;
+    uint32_t w = 0, h = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t begin_node = nullptr;  // k_frame_begin: the node whose parameters carry camera and scene
+    cudaKernelNodeParams begin_params{};
+    const uint32_t* final_pair_vals = nullptr;
+};
+
+void spl_frame_graph_destroy(spl_frame_graph* g) {
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+}
+
+int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, void* out_device, spl_frame_graph** out) {
+    if (!r || !out_device || !out) return fail(SPL_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    if (width == 0 || height == 0 || width > 65535 || height > 65535)
+        return fail(SPL_ERR_INVALID, "viewport %ux%u outside [1, 65535]", width, height);
+    if (r->profiling) return fail(SPL_ERR_INVALID, "turn profiling off before capturing a frame");
+    int rc = spl_renderer_reserve(r, width, height);
+    if (rc) return rc;
+    spl_frame_graph* g = new (std::nothrow) spl_frame_graph();
+    if (!g) return fail(SPL_ERR_OOM, "host allocation failed");
+    g->r = r;
+    g->w = width;
+    g->h = height;
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete g;
+        return fail(SPL_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    // The uniform block of this viewport with a placeholder pose: the raster's parameters (viewport,
+    // pixel size, margin) are taken from it on the host and baked into the graph; every launch
+    // replaces the whole block on the device (camera included) and the scene view.
+    const float pose[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, -5, 1};
+    Uniforms u;
+    compute_uniforms(r->cfg, pose, width, height, u);
+    const SceneView sv{};
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        rc = render_frame_impl(r, sv, u, width, height, out_device, cs, (uint32_t)r->max_n);
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &g->graph);
+        if (!rc && e2 != cudaSuccess) rc = fail(SPL_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
+    } else {
+        rc = fail(SPL_ERR_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+    }
+    cudaStreamDestroy(cs);
+    if (!rc) {
+        g->final_pair_vals = r->final_pair_vals;
+        size_t nn = 0;
+        e = cudaGraphGetNodes(g->graph, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (e == cudaSuccess && nn) e = cudaGraphGetNodes(g->graph, nodes.data(), &nn);
+        for (size_t i = 0; e == cudaSuccess && i < nn && !g->begin_node; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+            cudaKernelNodeParams kp{};
+            if (cudaGraphKernelNodeGetParams(nodes[i], &kp) == cudaSuccess && kp.func == frame_begin_kernel()) {
+                g->begin_node = nodes[i];
+                g->begin_params = kp;
+            }
+        }
+        if (e != cudaSuccess) rc = fail(SPL_ERR_CUDA, "cudaGraphGetNodes: %s", cudaGetErrorString(e));
+        else if (!g->begin_node) rc = fail(SPL_ERR_CUDA, "captured frame has no frame-begin node");
+    }
+    if (!rc) {
+        e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+        if (e != cudaSuccess) rc = fail(SPL_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    }
+    cudaGetLastError();
+    if (rc) {
+        spl_frame_graph_destroy(g);
+        return rc;
+    }
+    *out = g;
+    return SPL_OK;
+}
+
+int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16], void* stream) {
+    if (!g || !scene || !camera_to_world) return fail(SPL_ERR_INVALID, "NULL argument");
+    spl_renderer* r = g->r;
+    if (scene->n > r->max_n) return fail(SPL_ERR_INVALID, "scene larger than the renderer's max_splat_count");
+    Uniforms u;
+    compute_uniforms(r->cfg, camera_to_world, g->w, g->h, u);
+    SceneView sv = scene->view();
+    FrameCounters* fc = r->fc;
+    uint32_t* ep = r->epoch;
+    Uniforms* du = r->d_u;
+    SceneView* dsv = r->d_sv;
+    void* args[6] = {&fc, &ep, &u, &du, &sv, &dsv};
+    cudaKernelNodeParams kp = g->begin_params;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    CU(cudaGraphExecKernelNodeSetParams(g->exec, g->begin_node, &kp));
+    CU(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    r->last_stream = (cudaStream_t)stream;
+    r->last_scene = scene;
+    r->last_u = u;
+    r->has_frame = true;
+    r->last_w = g->w;
+    r->last_h = g->h;
+    r->last_n = scene->n;
+    r->final_pair_vals = g->final_pair_vals;
+    return SPL_OK;
+}
+
+int spl_scene_load_chunk_device(spl_scene* s, const float* records_device, uint64_t start, uint64_t count,
+                                void* stream) {
+    if (!s || (!records_device && count)) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (start >= s->n) return SPL_OK;
+    if (count > s->n - start) count = s->n - start;
+    for (uint64_t first = 0; first < count; first += 0x40000000ull) {
+        const uint64_t cnt = count - first < 0x40000000ull ? count - first : 0x40000000ull;
+        const uint64_t at = start + first;
+        launch_load_records(records_device + first * 62, (uint32_t)cnt, s->x + at, s->y + at, s->z + at, s->rot + at,
+                            s->scale_alpha + at, s->sh + at * 48, (cudaStream_t)stream);
+    }
+    CU(cudaGetLastError());
     return SPL_OK;
 }
 

@@ -17,7 +17,7 @@
 namespace spl {
 
 // ------------------------------------------------------------------------------------------------
-__global__ void k_frame_begin(FrameCounters* fc, uint32_t* epoch_word) {
+__device__ __forceinline__ void counters_begin(FrameCounters* fc, uint32_t* epoch_word) {
     uint32_t* w = reinterpret_cast<uint32_t*>(fc);
     const uint32_t nwords = sizeof(FrameCounters) / 4;
     for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) w[i] = 0u;
@@ -30,8 +30,39 @@ __global__ void k_frame_begin(FrameCounters* fc, uint32_t* epoch_word) {
     }
 }
 
+__global__ void k_counters_begin(FrameCounters* fc, uint32_t* epoch_word) { counters_begin(fc, epoch_word); }
+
+// A frame's first kernel: the counters as above, and the frame's uniform block and scene view
+// (kernel parameters here, so that a captured frame graph takes a new camera and scene by updating
+// this one node) published to device memory for the kernels that follow.
+__global__ void k_frame_begin(FrameCounters* fc, uint32_t* epoch_word, Uniforms u, Uniforms* d_u, SceneView sv,
+                              SceneView* d_sv) {
+    if (threadIdx.x < sizeof(Uniforms) / 4)
+        reinterpret_cast<uint32_t*>(d_u)[threadIdx.x] = reinterpret_cast<const uint32_t*>(&u)[threadIdx.x];
+    if (threadIdx.x < sizeof(SceneView) / 4)
+        reinterpret_cast<uint32_t*>(d_sv)[threadIdx.x] = reinterpret_cast<const uint32_t*>(&sv)[threadIdx.x];
+    counters_begin(fc, epoch_word);
+}
+
 void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st) {
-    k_frame_begin<<<1, 256, 0, st>>>(fc, epoch_word);
+    k_counters_begin<<<1, 256, 0, st>>>(fc, epoch_word);
+}
+
+void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, const Uniforms& u, Uniforms* d_u, const SceneView& sv,
+                        SceneView* d_sv, cudaStream_t st) {
+    k_frame_begin<<<1, 256, 0, st>>>(fc, epoch_word, u, d_u, sv, d_sv);
+}
+
+const void* frame_begin_kernel() { return reinterpret_cast<const void*>(&k_frame_begin); }
+
+// The frame's uniform block and scene view staged in shared memory (one word per thread of the
+// first warps; the caller synchronises).
+__device__ __forceinline__ void stage_frame(const Uniforms* __restrict__ d_u, Uniforms& s_u,
+                                            const SceneView* __restrict__ d_sv, SceneView& s_sv) {
+    if (threadIdx.x < sizeof(Uniforms) / 4)
+        reinterpret_cast<uint32_t*>(&s_u)[threadIdx.x] = __ldg(reinterpret_cast<const uint32_t*>(d_u) + threadIdx.x);
+    if (threadIdx.x < sizeof(SceneView) / 4)
+        reinterpret_cast<uint32_t*>(&s_sv)[threadIdx.x] = __ldg(reinterpret_cast<const uint32_t*>(d_sv) + threadIdx.x);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -39,22 +70,29 @@ void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st
 // splats [w*512, w*512+512) of the tile and lane l handles elements w*512 + 32*j + l, so loads are
 // coalesced and the ballot order is the index order.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_cull_key(SceneView s, Uniforms u, FrameCounters* fc,
+__global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict__ d_sv, const Uniforms* __restrict__ d_u,
+                                                  FrameCounters* fc,
                                                   const uint32_t* __restrict__ epoch_word, uint64_t* status,
                                                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ idx_out,
                                                   uint32_t spin_limit) {
     __shared__ uint32_t s_hist[1024];
     __shared__ uint32_t s_wcnt[8];
     __shared__ uint32_t s_tile, s_epoch, s_base;
+    __shared__ Uniforms s_u;
+    __shared__ SceneView s_sv;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     for (uint32_t i = tid; i < 1024u; i += 256u) s_hist[i] = 0u;
+    stage_frame(d_u, s_u, d_sv, s_sv);
     if (tid == 0) {
         s_tile = atomicAdd(&fc->tile_counter[0], 1u);
         s_epoch = *epoch_word;
     }
     __syncthreads();
+    const Uniforms& u = s_u;
+    const SceneView& s = s_sv;
     const uint32_t tile = s_tile, epoch = s_epoch, n = s.n;
     const uint32_t ntiles = (n + CULL_TILE - 1) / CULL_TILE;
+    if (tile >= ntiles) return;  // a grid sized for a larger scene (captured frames)
     const uint32_t base = tile * CULL_TILE + w * 512u + lane;
 
     float px[16], py[16], pz[16];
@@ -147,14 +185,15 @@ __global__ void __launch_bounds__(256) k_cull_key(SceneView s, Uniforms u, Frame
     }
 }
 
-void launch_cull_key(int mode, const SceneView& s, const Uniforms& u, FrameCounters* fc, const uint32_t* epoch_word,
-                     uint64_t* status, uint32_t* keys_out, uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st) {
-    if (s.n == 0) return;
-    const uint32_t grid = (s.n + CULL_TILE - 1) / CULL_TILE;
+void launch_cull_key(int mode, uint32_t grid_n, const SceneView* d_sv, const Uniforms* u, FrameCounters* fc,
+                     const uint32_t* epoch_word, uint64_t* status, uint32_t* keys_out, uint32_t* idx_out,
+                     uint32_t spin_limit, cudaStream_t st) {
+    if (grid_n == 0) return;
+    const uint32_t grid = (grid_n + CULL_TILE - 1) / CULL_TILE;
     if (mode == DS_CPU)
-        k_cull_key<DS_CPU><<<grid, 256, 0, st>>>(s, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
+        k_cull_key<DS_CPU><<<grid, 256, 0, st>>>(d_sv, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
     else
-        k_cull_key<DS_GPU><<<grid, 256, 0, st>>>(s, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
+        k_cull_key<DS_GPU><<<grid, 256, 0, st>>>(d_sv, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -174,9 +213,17 @@ __device__ __forceinline__ void load_sh(const float* __restrict__ sh, uint32_t i
 }
 
 template <int SHO, bool COV, bool RECT>
-__global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
+__global__ void __launch_bounds__(256) k_preprocess(const SceneView* __restrict__ d_sv,
+                                                    const Uniforms* __restrict__ d_u,
+                                                    const uint32_t* __restrict__ idx,
                                                     const FrameCounters* __restrict__ fc, float4* __restrict__ rec,
                                                     uint2* __restrict__ boxes) {
+    __shared__ Uniforms s_u;
+    __shared__ SceneView s_sv;
+    stage_frame(d_u, s_u, d_sv, s_sv);
+    __syncthreads();
+    const Uniforms& u = s_u;
+    const SceneView& s = s_sv;
     const uint32_t V = fc->visible;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < V; slot += gridDim.x * blockDim.x) {
         const uint32_t i = __ldg(idx + slot);
@@ -231,7 +278,7 @@ __global__ void __launch_bounds__(256) k_preprocess(SceneView s, Uniforms u, con
 }
 
 template <int SHO, bool COV>
-static void launch_pre2(bool rect, dim3 g, const SceneView& s, const Uniforms& u, const uint32_t* idx,
+static void launch_pre2(bool rect, dim3 g, const SceneView* s, const Uniforms* u, const uint32_t* idx,
                         const FrameCounters* fc, float4* rec, uint2* boxes, cudaStream_t st) {
     if (rect)
         k_preprocess<SHO, COV, true><<<g, 256, 0, st>>>(s, u, idx, fc, rec, boxes);
@@ -239,7 +286,7 @@ static void launch_pre2(bool rect, dim3 g, const SceneView& s, const Uniforms& u
         k_preprocess<SHO, COV, false><<<g, 256, 0, st>>>(s, u, idx, fc, rec, boxes);
 }
 template <int SHO>
-static void launch_pre1(bool cov, bool rect, dim3 g, const SceneView& s, const Uniforms& u, const uint32_t* idx,
+static void launch_pre1(bool cov, bool rect, dim3 g, const SceneView* s, const Uniforms* u, const uint32_t* idx,
                         const FrameCounters* fc, float4* rec, uint2* boxes, cudaStream_t st) {
     if (cov)
         launch_pre2<SHO, true>(rect, g, s, u, idx, fc, rec, boxes, st);
@@ -247,7 +294,7 @@ static void launch_pre1(bool cov, bool rect, dim3 g, const SceneView& s, const U
         launch_pre2<SHO, false>(rect, g, s, u, idx, fc, rec, boxes, st);
 }
 
-void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
+void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView* s, const Uniforms* u,
                        const uint32_t* idx, const FrameCounters* fc, float4* rec, uint2* boxes, uint32_t max_n,
                        cudaStream_t st) {
     if (max_n == 0) return;

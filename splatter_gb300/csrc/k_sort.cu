@@ -129,23 +129,35 @@ __global__ void __launch_bounds__(OS_THREADS, 3)
     }
 }
 
-static int g_os_blocks_per_sm = 0;
-static int g_num_sms = 0;
+struct OnesweepShape {
+    int num_sms = 1, blocks_per_sm = 1;
+};
+
+// Queried once per process (a function-local static: safe when several host threads launch).
+static const OnesweepShape& onesweep_shape() {
+    static const OnesweepShape shape = [] {
+        OnesweepShape s;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s.blocks_per_sm, k_onesweep<false>, OS_THREADS, 0);
+        if (s.blocks_per_sm < 1) s.blocks_per_sm = 1;
+        if (s.num_sms < 1) s.num_sms = 1;
+        return s;
+    }();
+    return shape;
+}
+
+void onesweep_prepare() { (void)onesweep_shape(); }
 
 void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                      const uint32_t* n_ptr, uint32_t n_cap, const uint32_t* hist256, uint64_t* status,
                      uint32_t* tile_counter, const uint32_t* epoch_word, int shift, uint32_t spin_limit,
                      uint32_t* err, cudaStream_t st) {
     if (n_cap == 0) return;
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_os_blocks_per_sm, k_onesweep<false>, OS_THREADS, 0);
-        if (g_os_blocks_per_sm < 1) g_os_blocks_per_sm = 1;
-    }
+    const OnesweepShape& shape = onesweep_shape();
     const uint32_t tiles = (n_cap + SORT_TILE - 1) / SORT_TILE;
-    uint32_t grid = (uint32_t)(g_num_sms * g_os_blocks_per_sm);
+    uint32_t grid = (uint32_t)(shape.num_sms * shape.blocks_per_sm);
     if (grid > tiles) grid = tiles;
     if (vals_in == nullptr)
         k_onesweep<true><<<grid, OS_THREADS, 0, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, n_cap, hist256,

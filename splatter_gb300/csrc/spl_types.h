@@ -68,14 +68,21 @@ struct SceneView {
 };
 
 // ---- launchers (defined in the .cu files) --------------------------------------------------------
-void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st);
-void launch_cull_key(int mode, const SceneView& s, const Uniforms& u, FrameCounters* fc, const uint32_t* epoch_word,
+void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st);  // counters + epoch only
+void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, const Uniforms& u, Uniforms* d_u, const SceneView& sv,
+                        SceneView* d_sv, cudaStream_t st);
+const void* frame_begin_kernel();  // host handle of k_frame_begin (to find its node in a captured graph)
+// grid_n: the splat count the grid is sized for (the scene's, or the renderer's maximum for a
+// captured frame whose scene changes between launches); the kernels read the scene from d_sv.
+void launch_cull_key(int mode, uint32_t grid_n, const SceneView* d_sv, const Uniforms* d_u, FrameCounters* fc,
+                     const uint32_t* epoch_word,
                      uint64_t* status, uint32_t* keys_out, uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st);
-void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
+void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView* d_sv, const Uniforms* d_u,
                        const uint32_t* idx, const FrameCounters* fc, float4* rec, uint2* boxes, uint32_t max_n,
                        cudaStream_t st);
 // One LSD onesweep pass over 8 bits at `shift`.  n = min(*n_ptr, n_cap).  vals_in == nullptr means
 // values are the input positions (0, 1, 2, ...).
+void onesweep_prepare();  // runs the one-time occupancy query outside any stream capture
 void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                      const uint32_t* n_ptr, uint32_t n_cap, const uint32_t* hist256, uint64_t* status,
                      uint32_t* tile_counter, const uint32_t* epoch_word, int shift, uint32_t spin_limit,

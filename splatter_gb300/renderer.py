@@ -21,7 +21,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import SplatterError, check
+from ._lib import SORT_COOPERATIVE, SORT_ONESWEEP, SplatterError, check
 
 __all__ = ["DepthSorting", "BlendMode", "Configuration", "Renderer", "Scene", "SplatterError", "FrameInfo",
            "compute_uniforms"]
@@ -187,6 +187,21 @@ class Renderer:
     def set_profiling(self, enable=True):
         check(self._lib.spl_renderer_set_profiling(self._h, 1 if enable else 0))
 
+    def set_sort_mode(self, mode):
+        """SORT_COOPERATIVE (default, one frame on the device at a time) or SORT_ONESWEEP (safe with
+        frames of other renderers running concurrently)."""
+        check(self._lib.spl_renderer_set_sort_mode(self._h, int(mode)))
+
+    def capture_frame(self, width, height, out=None):
+        """A frame at width x height captured into a CUDA graph writing into `out` (allocated if
+        None); FrameGraph.launch(scene, camera) replays it for any scene and camera."""
+        if out is None:
+            out = self.output_buffer(width, height)
+        h = ctypes.c_void_p()
+        check(self._lib.spl_frame_graph_create(self._h, int(width), int(height), ctypes.c_void_p(out.data_ptr()),
+                                               ctypes.byref(h)))
+        return FrameGraph(self, out, h)
+
     def stage_times(self):
         """{stage: milliseconds} of the last frame (needs set_profiling(True) before the frame)."""
         arr = (ctypes.c_float * len(_lib.STAGES))()
@@ -206,6 +221,31 @@ class Renderer:
                                        ctypes.c_void_p(ko.data_ptr()), ctypes.c_void_p(vo.data_ptr()), n,
                                        int(key_bits), _stream_ptr(stream)))
         return ko, vo
+
+
+class FrameGraph:
+    """A captured frame (spl_frame_graph_*); keeps its renderer and output alive."""
+
+    def __init__(self, renderer, out, handle):
+        self._lib = _lib.load()
+        self.renderer, self.out, self._h = renderer, out, handle
+
+    def launch(self, scene, camera_to_world, stream=None):
+        cam = _cam(camera_to_world)
+        check(self._lib.spl_frame_graph_launch(self._h, scene.handle, cam.ctypes.data_as(ctypes.c_void_p),
+                                               _stream_ptr(stream)))
+        return self.out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.spl_frame_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Scene:
@@ -267,6 +307,13 @@ class Scene:
         rec = np.ascontiguousarray(records, dtype=np.float32).reshape(-1, 62)
         check(self._lib.spl_scene_load_chunk(self._h, rec.ctypes.data_as(ctypes.c_void_p), int(start), rec.shape[0],
                                              _stream_ptr(stream)))
+
+    def load_chunk_device(self, records, start=0, stream=None):
+        """Scene::load_chunk from a CUDA float32 tensor of (K, 62) records (no staging)."""
+        assert records.is_cuda and records.dtype.itemsize == 4 and records.is_contiguous()
+        k = records.numel() // 62
+        check(self._lib.spl_scene_load_chunk_device(self._h, ctypes.c_void_p(records.data_ptr()), int(start), k,
+                                                    _stream_ptr(stream)))
 
     def load_chunk_file(self, path, header_bytes, start, count, stream=None):
         """Scene::load_chunk reading records from a splat file."""

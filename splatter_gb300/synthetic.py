@@ -7,6 +7,7 @@ of the benchmark configurations:
 * ``plain_small``   100k splats, positions ~ N(0, 2^2), SH degree 0 (640x480, fovy 60 deg).
 * ``clustered``     64 Gaussian clusters (sigma 0.5-3, centres uniform in the 40^3 box) plus 20%
                     uniform background, SH degree 3 (band 0 ~ N(0, 0.3^2), higher ~ N(0, 0.05^2)).
+                    ``clustered_device`` draws the same distributions on the GPU (serving scenes).
 
 Every generator returns PLY-layout records, shape (N, 62) float32 (scene.rs:15-24): centre[3],
 normal[3], colour[48] (coefficient k of channel c at 3k+c, the slot the shader reads,
@@ -18,8 +19,8 @@ import math
 
 import numpy as np
 
-__all__ = ["RECORD_FLOATS", "plain_small", "clustered", "records_to_splats60", "dev_test_splats60",
-           "serving_scene_sizes"]
+__all__ = ["RECORD_FLOATS", "plain_small", "clustered", "clustered_device", "records_to_splats60",
+           "dev_test_splats60", "serving_scene_sizes"]
 
 RECORD_FLOATS = 62
 
@@ -64,6 +65,39 @@ def clustered(n=1_000_000, seed=1, sh_order=3, clusters=64, background=0.2, box=
     perm = rng.permutation(n)
     centers = centers[perm]
     return _records(n, rng, centers, sh_order)
+
+
+def clustered_device(n, seed=1, sh_order=3, clusters=64, background=0.2, box=40.0, device="cuda"):
+    """``clustered`` generated on the GPU with torch's generator (same distributions, a different
+    random stream): a (n, 62) float32 CUDA tensor of file records."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    f32 = dict(device=device, dtype=torch.float32)
+    nb = int(round(n * background))
+    nc = n - nb
+    cc = (torch.rand((clusters, 3), generator=g, **f32) - 0.5) * box
+    cs = 0.5 + 2.5 * torch.rand(clusters, generator=g, **f32)
+    which = torch.randint(0, clusters, (nc,), generator=g, device=device)
+    rec = torch.zeros((n, RECORD_FLOATS), **f32)
+    centers = torch.empty((n, 3), **f32)
+    centers[:nc] = cc[which] + torch.randn((nc, 3), generator=g, **f32) * cs[which, None]
+    centers[nc:] = (torch.rand((nb, 3), generator=g, **f32) - 0.5) * box
+    rec[:, 0:3] = centers[torch.randperm(n, generator=g, device=device)]
+    rec[:, 6:9] = 0.3 * torch.randn((n, 3), generator=g, **f32)
+    if sh_order > 0:
+        ncoef = (sh_order + 1) ** 2
+        rec[:, 9:6 + 3 * ncoef] = 0.05 * torch.randn((n, 3 * ncoef - 3), generator=g, **f32)
+    rec[:, 54] = 1.5 * torch.randn(n, generator=g, **f32)
+    rec[:, 55:58] = -4.0 + 0.5 * torch.randn((n, 3), generator=g, **f32)
+    u = torch.rand((n, 3), generator=g, **f32)
+    a = torch.sqrt(1.0 - u[:, 0])
+    b = torch.sqrt(u[:, 0])
+    rec[:, 58] = a * torch.sin(2 * math.pi * u[:, 1])
+    rec[:, 59] = a * torch.cos(2 * math.pi * u[:, 1])
+    rec[:, 60] = b * torch.sin(2 * math.pi * u[:, 2])
+    rec[:, 61] = b * torch.cos(2 * math.pi * u[:, 2])
+    return rec
 
 
 def records_to_splats60(center, rotation, scale, alpha, sh):

@@ -70,3 +70,28 @@ def test_record_gradients_chain_to_parameter_gradients():
         checked += 1
     g.close()
     assert checked > 100
+
+
+def test_pinned_records_reproduce_the_oracles_own():
+    """pin_records with the oracle's own FP64 records rounded to FP32 changes the record gradients
+    only at FP32 rounding level."""
+    n = 800
+    rec = synthetic.plain_small(n, seed=5, sh_order=3)
+    rec[:, 55:58] += 1.0
+    sc = {k: v.astype(np.float64) for k, v in oracle.load_transform(rec).items()}
+    W, H = 64, 48
+    cam = camera.look_at([0.4, 0.6, -7.0], [0.0, 0.0, 0.0])
+    u = oracle.uniforms(cam, W, H, fovy=math.radians(60))
+    cfg = oracle.config_struct(depth_sorting=2, sh_order=3, blend_mode=1)
+    g = oracle.GradContext(u, cfg, sc, np.full((H, W, 3), 0.3))
+    rg0, order = g.record_gradients(threads=4)
+    sc32 = {k: v.astype(np.float32) for k, v in sc.items()}
+    recs, _, _ = oracle.preprocess(u, cfg, sc32, order, fp64=True)
+    g.pin_records(recs, order)
+    rg1, order1 = g.record_gradients(threads=4)
+    g.close()
+    assert np.array_equal(order, order1)
+    live = np.abs(rg0).sum(1) > 0
+    assert live.sum() > 100
+    scale = np.maximum(np.abs(rg0[live]), 1e-3 * np.abs(rg0[live]).max(0))
+    assert np.mean(np.abs(rg1[live] - rg0[live]) / scale <= 1e-3) >= 0.99

@@ -244,13 +244,14 @@ SPL_API int spl_renderer_set_sort_mode(spl_renderer* r, int mode);
 
 /* ---- captured frames (extension) ----------------------------------------------------------------
  * A frame at width x height into `out_device`, captured once into a CUDA graph with grids sized for
- * the renderer's max_splat_count; each launch replays it for any scene and camera (only the first
- * kernel's parameters change: the kernels read the scene and every count from device memory), on
- * any stream.  The renderer's scratch is shared with its other frames: one frame of a renderer in
- * flight at a time.  Destroy the graph before the renderer or the output buffer. */
+ * scenes of up to max_splats splats (0: the renderer's max_splat_count); each launch replays it for
+ * any such scene and any camera (only the first kernel's parameters change: the kernels read the
+ * scene and every count from device memory), on any stream.  The renderer's scratch is shared with
+ * its other frames: one frame of a renderer in flight at a time.  Destroy the graph before the
+ * renderer or the output buffer. */
 typedef struct spl_frame_graph spl_frame_graph;
-SPL_API int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, void* out_device,
-                                   spl_frame_graph** out);
+SPL_API int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, uint64_t max_splats,
+                                   void* out_device, spl_frame_graph** out);
 SPL_API int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16],
                                    void* stream);
 SPL_API void spl_frame_graph_destroy(spl_frame_graph* g);
@@ -265,7 +266,7 @@ SPL_API int spl_scene_load_chunk_device(spl_scene* s, const float* records_devic
  * on the next request).  Requests of any scene, pose and viewport are admitted continuously as
  * slots free up: each slot owns a renderer's scratch, a stream and an output buffer, so the frames
  * of different slots overlap on the device; with use_graphs each slot replays a captured frame
- * graph per viewport.  One scheduler thread per server issues all device work. */
+ * graph per viewport and power-of-two scene-size class (grids at most twice the scene).  One scheduler thread per server issues all device work. */
 typedef struct spl_server spl_server;
 typedef struct spl_server_config {
     uint32_t slots;               /* frames in flight (>= 1) */

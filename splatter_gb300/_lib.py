@@ -134,7 +134,7 @@ SIGNATURES = [
     ("spl_render_backward", I32, [P, P, P, P, P, P, P, P, P, P, P]),
     ("spl_renderer_copy_record_gradients", I32, [P, P, U64, P]),
     ("spl_renderer_set_sort_mode", I32, [P, I32]),
-    ("spl_frame_graph_create", I32, [P, U32, U32, P, ctypes.POINTER(P)]),
+    ("spl_frame_graph_create", I32, [P, U32, U32, U64, P, ctypes.POINTER(P)]),
     ("spl_frame_graph_launch", I32, [P, P, P, P]),
     ("spl_frame_graph_destroy", None, [P]),
     ("spl_scene_load_chunk_device", I32, [P, P, U64, U64, P]),

@@ -787,6 +787,7 @@ int spl_parse_file_header(const char* path, uint32_t* header_bytes, uint64_t* sp
 struct spl_frame_graph {
     spl_renderer* r = nullptr;
     uint32_t w = 0, h = 0;
+    uint64_t max_splats = 0;  // the grids' bound
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t begin_node = nullptr;  // k_frame_begin: the node whose parameters carry camera and scene
@@ -801,9 +802,11 @@ void spl_frame_graph_destroy(spl_frame_graph* g) {
     delete g;
 }
 
-int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, void* out_device, spl_frame_graph** out) {
+int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, uint64_t max_splats, void* out_device,
+                           spl_frame_graph** out) {
     if (!r || !out_device || !out) return fail(SPL_ERR_INVALID, "NULL argument");
     *out = nullptr;
+    if (max_splats == 0 || max_splats > r->max_n) max_splats = r->max_n;
     if (width == 0 || height == 0 || width > 65535 || height > 65535)
         return fail(SPL_ERR_INVALID, "viewport %ux%u outside [1, 65535]", width, height);
     if (r->profiling) return fail(SPL_ERR_INVALID, "turn profiling off before capturing a frame");
@@ -814,6 +817,7 @@ int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, voi
     g->r = r;
     g->w = width;
     g->h = height;
+    g->max_splats = max_splats;
     cudaStream_t cs = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -829,7 +833,7 @@ int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, voi
     const SceneView sv{};
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        rc = render_frame_impl(r, sv, u, width, height, out_device, cs, (uint32_t)r->max_n);
+        rc = render_frame_impl(r, sv, u, width, height, out_device, cs, (uint32_t)max_splats);
         const cudaError_t e2 = cudaStreamEndCapture(cs, &g->graph);
         if (!rc && e2 != cudaSuccess) rc = fail(SPL_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
     } else {
@@ -870,7 +874,9 @@ int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, voi
 int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16], void* stream) {
     if (!g || !scene || !camera_to_world) return fail(SPL_ERR_INVALID, "NULL argument");
     spl_renderer* r = g->r;
-    if (scene->n > r->max_n) return fail(SPL_ERR_INVALID, "scene larger than the renderer's max_splat_count");
+    if (scene->n > g->max_splats)
+        return fail(SPL_ERR_INVALID, "scene of %llu splats exceeds the graph's bound %llu",
+                    (unsigned long long)scene->n, (unsigned long long)g->max_splats);
     Uniforms u;
     compute_uniforms(r->cfg, camera_to_world, g->w, g->h, u);
     SceneView sv = scene->view();

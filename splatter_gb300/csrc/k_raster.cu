@@ -161,17 +161,34 @@ void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint
 // ------------------------------------------------------------------------------------------------
 constexpr int RASTER_BATCH = 256;
 
-// One CTA per 16x16 tile, one thread per pixel.  Warp w owns rows 2w, 2w+1, split into four 4x2-pixel
-// groups of 8 lanes (group g = lane / 8 covers columns 4g..4g+3).  The tile's records (depth order)
+// One CTA per 16x16 tile, one thread per pixel.  Warp w owns rows 2w, 2w+1, split into eight 2x2-pixel
+// groups of 4 lanes (group g = lane / 4 covers columns 2g, 2g+1).  The tile's records (depth order)
 // are staged through shared memory in batches of 256.  For each chunk of 32 records a lane tests one
-// record's pixel box against the four groups' blocks; four ballots give each group its relevance
-// list, in order.  The warp then walks the four lists at once: in every iteration each group takes
-// its next record, so one pass of the per-pixel code serves up to four splats (most splats here
-// cover a few pixels, so this keeps far more lanes busy than a whole warp per splat).  Per pixel:
-// box test, coverage test, falloff, 1/255 discard, blend — the operations of the oracle's
+// record's pixel box against the eight groups' blocks; eight ballots give each group its relevance
+// list, in order.  The warp then walks the eight lists at once: in every iteration each group takes
+// its next record, so one pass of the per-pixel code serves up to eight splats (most splats here
+// cover a few pixels, so small groups keep far more lanes busy than a whole warp per splat).  Per
+// pixel: box test, coverage test, falloff, 1/255 discard, blend — the operations of the oracle's
 // raster_tile in the same order, so the image is bit-identical.  Lists are walked in depth order per
 // pixel, a warp whose pixels are all finished skips the rest, and the CTA stops once every pixel is
 // finished (T == 0 in unorm8 mode, T < 1e-4 in fp32 mode).
+// Block indices g (of the eight along a warp's strip) with |c + s g| <= T, widened conservatively:
+// the quotients are clamped to [-1, 9] before rounding outwards, so their float error (a few ulp of
+// at most 9) stays far below the 1e-3 widening.  Empty when lo > hi.
+__device__ __forceinline__ void g_interval(float c, float s, float T, int& lo, int& hi) {
+    if (fabsf(s) < 1e-30f) {
+        const bool all = fabsf(c) <= T;
+        lo = all ? -1 : 1;
+        hi = all ? 9 : 0;
+        return;
+    }
+    const float rs = 1.0f / s;  // IEEE: finite and within half an ulp for every finite s here
+    const float q1 = (-T - c) * rs, q2 = (T - c) * rs;
+    const float a = fminf(fmaxf(fminf(q1, q2), -1.0f), 9.0f), b = fminf(fmaxf(fmaxf(q1, q2), -1.0f), 9.0f);
+    lo = (int)ceilf(a - 1e-3f);
+    hi = (int)floorf(b + 1e-3f);
+}
+
 template <bool RECT, int BLEND>
 __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ pair_vals,
                                                 const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
@@ -180,12 +197,12 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     __shared__ float4 s_q3[RECT ? 1 : RASTER_BATCH];
     __shared__ float s_lut[256];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
-    const uint32_t grp = lane >> 3, li = lane & 7u;
+    const uint32_t grp = lane >> 2, li = lane & 3u;
     const int tile = blockIdx.x;
     const int tx = tile % tiles_x, ty = tile / tiles_x;
-    const int bx0 = tx * TILE_PIXELS + 4 * (int)grp;  // this lane's 4x2 block
+    const int bx0 = tx * TILE_PIXELS + 2 * (int)grp;  // this lane's 2x2 block
     const int by0 = ty * TILE_PIXELS + 2 * (int)w;
-    const int px = bx0 + (int)(li & 3u), py = by0 + (int)(li >> 2);
+    const int px = bx0 + (int)(li & 1u), py = by0 + (int)(li >> 1);
     const float X = (float)px + 0.5f, Y = (float)py + 0.5f;
     s_lut[tid] = (float)tid / 255.0f;
     const uint2 rg = ranges[tile];
@@ -195,7 +212,7 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     int cr = 0, cg = 0, cb = 0, ta = 255;
     float fr = 0.0f, fg = 0.0f, fb = 0.0f, ft = 1.0f;
     const float alpha_min = 1.0f / 255.0f;
-    const int wx0 = tx * TILE_PIXELS;  // the four blocks of this warp: columns wx0 + 4g .. + 3, rows by0, by0+1
+    const int wx0 = tx * TILE_PIXELS;  // the eight blocks of this warp: columns wx0 + 2g, + 1, rows by0, by0+1
     for (uint32_t b = rg.x; b < rg.y; b += RASTER_BATCH) {
         __syncthreads();
         const uint32_t i = b + tid;
@@ -211,25 +228,56 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
         const uint32_t cnt = min((uint32_t)RASTER_BATCH, rg.y - b);
         if (!warp_done) {
             for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
-                // relevance of record j0 + lane for each of the warp's four blocks
-                uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+                // pixels finished: the warp leaves, a finished 2x2 group walks no list
+                const uint32_t dmask = __ballot_sync(FULL_MASK, done);
+                if (dmask == FULL_MASK) break;
+                const bool grp_done = ((dmask >> (4u * grp)) & 0xFu) == 0xFu;
+                // relevance of record j0 + lane for each of the warp's eight blocks as an interval
+                // [ga, gb] of block indices; `mine` keeps the ballot of this lane's block.  A block is
+                // relevant when the record's pixel box meets it and, for rectangles, when some pixel
+                // centre of it may lie in the rectangle: over the block's four centres tc lies within
+                // tc(block centre) +- ext (half the block's extent mapped by |A|, widened by a rounding
+                // bound far above the per-pixel FMA chains' error), and along the warp's strip the
+                // block centre's tc is c + 2g A, so |c + 2g A| <= margin + ext is an interval of g.
+                // Skipped blocks hold no drawn pixel: the image is unchanged.
+                int ga = 1, gb = 0;
                 {
                     const uint32_t jl = j0 + lane;
-                    int x0 = 1, x1 = 0, y0 = 1, y1 = 0;
                     if (jl < cnt) {
-                        const uint32_t lo = __float_as_uint(s_q1[jl].w), hi = __float_as_uint(s_q2[jl].w);
-                        x0 = (int)(lo & 0xFFFFu);
-                        y0 = (int)(lo >> 16);
-                        x1 = (int)(hi & 0xFFFFu);
-                        y1 = (int)(hi >> 16);
+                        const float4 r1 = s_q1[jl];
+                        const uint32_t lo = __float_as_uint(r1.w), hi = __float_as_uint(s_q2[jl].w);
+                        const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
+                        const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
+                        if (!(y1 < by0 || y0 > by0 + 1) && x0 <= x1) {
+                            // block g covers columns wx0 + 2g, wx0 + 2g + 1 (floor halves: arithmetic shifts)
+                            ga = (x0 - wx0) >> 1;
+                            gb = (x1 - wx0) >> 1;
+                            if (RECT) {
+                                const float4 r0 = s_q0[jl];
+                                const float Xc = (float)(wx0 + 1), Yc = (float)(by0 + 1);  // block 0's centre
+                                const float Xm = (float)(wx0 + 16), Ym = (float)(by0 + 2);
+                                const float cx = fmaf(r0.y, Yc, fmaf(r0.x, Xc, r0.z));
+                                const float cy = fmaf(r1.x, Yc, fmaf(r0.w, Xc, r1.y));
+                                const float Tx = margin + 0.5f * (fabsf(r0.x) + fabsf(r0.y)) +
+                                                 1e-6f * (fabsf(r0.x) * Xm + fabsf(r0.y) * Ym + fabsf(r0.z));
+                                const float Ty = margin + 0.5f * (fabsf(r0.w) + fabsf(r1.x)) +
+                                                 1e-6f * (fabsf(r0.w) * Xm + fabsf(r1.x) * Ym + fabsf(r1.y));
+                                int lx, hx, ly, hy;
+                                g_interval(cx, 2.0f * r0.x, Tx, lx, hx);
+                                g_interval(cy, 2.0f * r0.w, Ty, ly, hy);
+                                ga = max(ga, max(lx, ly));
+                                gb = min(gb, min(hx, hy));
+                            }
+                        }
                     }
-                    const bool rows = !(y1 < by0 || y0 > by0 + 1) && x0 <= x1;
-                    m0 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 0 || x0 > wx0 + 3));
-                    m1 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 4 || x0 > wx0 + 7));
-                    m2 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 8 || x0 > wx0 + 11));
-                    m3 = __ballot_sync(FULL_MASK, rows && !(x1 < wx0 + 12 || x0 > wx0 + 15));
                 }
-                uint32_t mine = grp == 0 ? m0 : (grp == 1 ? m1 : (grp == 2 ? m2 : m3));
+                uint32_t mine = 0u;
+#pragma unroll
+                for (int g = 0; g < 8; ++g) {
+                    const uint32_t m = __ballot_sync(FULL_MASK, ga <= g && g <= gb);
+                    mine = (int)grp == g ? m : mine;
+                }
+                if (grp_done) mine = 0u;
                 while (__any_sync(FULL_MASK, mine != 0u)) {
                     if (mine == 0u) continue;
                     const uint32_t j = j0 + (uint32_t)(__ffs(mine) - 1);

@@ -9,8 +9,8 @@
 //
 // Requests: a FIFO queue filled by spl_server_submit from any thread.  One scheduler thread admits
 // the head request whenever a slot is free (continuous admission: no batch boundary), renders it on
-// the slot's stream (a captured frame graph per viewport, launched with the request's scene and
-// camera, or direct launches), copies the image and the frame's error word to the host, and
+// the slot's stream (a captured frame graph per viewport and scene-size class, launched with the
+// request's scene and camera, or direct launches), copies the image and the frame's error word to the host, and
 // queues a host callback that marks the slot done and wakes the scheduler.  Slots share nothing on the device but the
 // scene arrays they read, so the frames of different slots overlap.
 #include <algorithm>
@@ -62,7 +62,16 @@ struct ServerScene {
     }
 };
 
-using GraphKey = std::pair<uint32_t, uint32_t>;  // viewport width, height
+using GraphKey = std::tuple<uint32_t, uint32_t, uint64_t>;  // viewport width, height, scene-size class
+
+// Grids of a captured frame are sized for the size class: the next power of two of the scene's
+// splat count (at least 2^16, at most the renderer's maximum), so a small scene does not launch the
+// empty CTAs of the largest one.
+uint64_t size_class(uint64_t n, uint64_t max_n) {
+    uint64_t c = 1ull << 16;
+    while (c < n) c <<= 1;
+    return c < max_n ? c : max_n;
+}
 
 struct Slot {
     spl_server* owner = nullptr;
@@ -242,11 +251,12 @@ void launch(spl_server* s, Slot* slot, const Pending& p, ServerScene* sc, bool r
         rc = spl::fail(SPL_ERR_CUDA, "cudaStreamWaitEvent failed");
     }
     if (!rc && s->scfg.use_graphs) {
-        const GraphKey key{req.width, req.height};
+        const uint64_t cls = size_class(sc->n, s->cfg.max_splat_count);
+        const GraphKey key{req.width, req.height, cls};
         auto it = slot->graphs.find(key);
         if (it == slot->graphs.end()) {
             spl_frame_graph* g = nullptr;
-            rc = spl_frame_graph_create(slot->r, req.width, req.height, slot->d_out, &g);
+            rc = spl_frame_graph_create(slot->r, req.width, req.height, cls, slot->d_out, &g);
             if (!rc) {
                 it = slot->graphs.emplace(key, g).first;
                 s->graphs_captured.fetch_add(1);

@@ -192,14 +192,15 @@ class Renderer:
         frames of other renderers running concurrently)."""
         check(self._lib.spl_renderer_set_sort_mode(self._h, int(mode)))
 
-    def capture_frame(self, width, height, out=None):
+    def capture_frame(self, width, height, out=None, max_splats=0):
         """A frame at width x height captured into a CUDA graph writing into `out` (allocated if
-        None); FrameGraph.launch(scene, camera) replays it for any scene and camera."""
+        None), grids sized for scenes of up to max_splats splats (0: max_splat_count);
+        FrameGraph.launch(scene, camera) replays it for any such scene and any camera."""
         if out is None:
             out = self.output_buffer(width, height)
         h = ctypes.c_void_p()
-        check(self._lib.spl_frame_graph_create(self._h, int(width), int(height), ctypes.c_void_p(out.data_ptr()),
-                                               ctypes.byref(h)))
+        check(self._lib.spl_frame_graph_create(self._h, int(width), int(height), int(max_splats),
+                                               ctypes.c_void_p(out.data_ptr()), ctypes.byref(h)))
         return FrameGraph(self, out, h)
 
     def stage_times(self):

@@ -54,6 +54,16 @@ def test_frame_graph_and_onesweep_match_direct(cuda):
         torch.cuda.synchronize()
         assert torch.equal(out.cpu(), want)
     g.close()
+    # a graph bounded to small scenes: same bytes, and larger scenes are refused
+    gs = r2.capture_frame(W, H, max_splats=10000)
+    for p in poses[:2]:
+        want = r.render_frame(s3_alone, p, W, H).cpu()
+        out = gs.launch(s3, p)
+        torch.cuda.synchronize()
+        assert torch.equal(out.cpu(), want)
+    with pytest.raises(SplatterError):
+        gs.launch(s2, poses[0])
+    gs.close()
 
 
 def _scene_on(renderer, rec):

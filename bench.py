@@ -200,15 +200,19 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic():
-    """Per-stage DRAM bytes per launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(path):
-        try:
-            return json.load(open(path))
-        except Exception:
-            return {}
-    return {}
+# DRAM traffic per unit of the dominant kernel, from one ncu capture of a smaller case of the same
+# workload (profiles/k_raster_3m_1080p.md: 3M splats, 1920x1080, 3,353,969 pairs, 235.7 MB read + 9.4
+# MB written): the reads grow with the pairs, the image write is per launch.  The bench scales it to
+# its own frames by their pair counts.
+TRAFFIC_PER_UNIT = {"raster": {"per_pair": 235.7e6 / 3353969.0, "per_launch": 9.4e6,
+                               "source": "profiles/k_raster_3m_1080p.md (3M-splat capture, scaled by pairs)"}}
+
+
+def stage_traffic(stage, P):
+    t = TRAFFIC_PER_UNIT.get(stage)
+    if not t:
+        return None
+    return int(t["per_pair"] * P + t["per_launch"])
 
 
 def stage_bytes(stage, V, D, P, N, W, H, sh_order=3):
@@ -294,12 +298,14 @@ def run_ours(args):
     stage_ms = {}
     stage_bytes_sum = {}
     vis_tot = 0
+    pairs_tot = 0
     frames_prof = min(args.steps, len(poses))
     for k in range(frames_prof):
         frame(args.warmup + k)
         st = r.stage_times()
         info = r.frame_info()
         vis_tot += info.visible_count
+        pairs_tot += info.pair_count
         for name, ms in st.items():
             stage_ms[name] = stage_ms.get(name, 0.0) + ms
             stage_bytes_sum[name] = stage_bytes_sum.get(name, 0) + stage_bytes(
@@ -314,10 +320,11 @@ def run_ours(args):
         gbs = stage_bytes_sum[name] / (stage_ms[name] / 1000.0) / 1e9 if stage_ms[name] > 0 else 0.0
         stages[name] = {"ms": round(avg_ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
     dominant = max(stages, key=lambda n: stages[n]["ms"])
-    traffic = load_traffic().get(dominant)
+    traffic = stage_traffic(dominant, pairs_tot / frames_prof)
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": stages[dominant]["gbs"], "peak": peak,
                 "unit": "GB/s", "frac": stages[dominant]["frac"], "peak_kind": f"{peak_kind} hbm_gbs",
-                "traffic": traffic, "algorithmic_bytes_per_launch": int(stage_bytes_sum[dominant] / frames_prof)}
+                "traffic": traffic, "traffic_source": TRAFFIC_PER_UNIT.get(dominant, {}).get("source"),
+                "algorithmic_bytes_per_launch": int(stage_bytes_sum[dominant] / frames_prof)}
 
     # ---- end to end through the public API with host buffers ----
     host = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)

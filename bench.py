@@ -14,6 +14,10 @@ Arms:
                      from the oracle's C restatement: the reference itself (Rust + wgpu) cannot be
                      built or run here
 
+Keys beside the contract's: `uhd` (the same fly-through at 3840x2160), `serving` (served vs plain
+loop, p50/p99 latency, byte-identity of the results), `differentiation` (forward+backward ms per
+iteration), `stages` (per-stage CUDA-event times and achieved GB/s).
+
 Multi-GPU: a frame does not shard (depth order is global), so --gpus N runs N independent replicas
 (one rank per GPU, no collective on the data path); value = frames of all ranks / max rank time.
 """
@@ -50,6 +54,7 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-differentiation", action="store_true", help="skip the forward+backward leg")
     p.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain leg")
+    p.add_argument("--no-uhd", action="store_true", help="skip the 3840x2160 measurement")
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-requests", type=int, default=800, help="closed-loop requests per loop")
     p.add_argument("--serve-rates", default="250,1000,2000", help="Poisson arrival rates (req/s)")
@@ -349,6 +354,25 @@ def run_ours(args):
 
     launches = r.launches_per_frame(W, H) * args.steps
 
+    # the same fly-through at 3840x2160 (the workload's second viewport), device-timed
+    uhd = None
+    if rank == 0 and not args.no_uhd:
+        W4, H4 = 3840, 2160
+        r.reserve(W4, H4)
+        out4 = r.output_buffer(W4, H4)
+        for k in range(args.warmup):
+            r.render_frame(s, poses[k % len(poses)], W4, H4, out=out4, stream=stream)
+        u0, u1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        u0.record(stream)
+        for k in range(args.steps):
+            r.render_frame(s, poses[(args.warmup + k) % len(poses)], W4, H4, out=out4, stream=stream)
+        u1.record(stream)
+        torch.cuda.synchronize()
+        ms4 = u0.elapsed_time(u1) / args.steps
+        uhd = {"width": W4, "height": H4, "frames_per_s": round(1000.0 / ms4, 2), "ms_per_step": round(ms4, 4),
+               "steps": args.steps}
+        del out4
+
     diff = None
     if rank == 0 and world == 1 and not args.no_differentiation:
         diff = run_differentiation(args)
@@ -374,7 +398,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "splats_per_s": round(value * args.splats, 0),
             "stages": stages, "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-            "cpu_baseline": cpu, "differentiation": diff, "serving": serving,
+            "cpu_baseline": cpu, "uhd": uhd, "differentiation": diff, "serving": serving,
         }
         s_line = json.dumps(line)
         print(s_line, flush=True)

@@ -248,3 +248,19 @@ def test_clustered_1m_1080p_parity(cuda):
         o = oracle_frame(config, sc, cam, 1920, 1080)
         assert_frame_parity(g, o, config)
         assert image_psnr(g[0], o[0]) == float("inf")
+
+
+@pytest.mark.parametrize("w,h,pose", [(1920, 1080, 0), (3840, 2160, 64)], ids=["1080p", "2160p"])
+def test_clustered_6m_flythrough_parity(cuda, w, h, pose):
+    """Config 'plain path at scale': 6M clustered splats, SH 3, ~40% culled, fly-through poses whose
+    near plane cuts through clusters, at 1920x1080 and 3840x2160: keys, visible set, permutation,
+    records and image bit-exact against the oracle."""
+    n = 6_000_000
+    config = Configuration(max_splat_count=n, spherical_harmonics_order=3, field_of_view_y=math.radians(60))
+    rec = synthetic.clustered(n, seed=2)
+    sc = oracle.load_transform(rec)
+    cam = camera.flythrough_poses(128, seed=9)[pose]
+    g = gpu_frame(cuda, config, rec, cam, w, h)
+    o = oracle_frame(config, sc, cam, w, h)
+    assert 0.3 * n < o[3] < 0.9 * n  # part of the scene culled
+    assert_frame_parity(g, o, config)

@@ -58,7 +58,7 @@ def parse_args(argv=None):
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-requests", type=int, default=800, help="closed-loop requests per loop")
     p.add_argument("--serve-rates", default="250,1000,2000", help="Poisson arrival rates (req/s)")
-    p.add_argument("--serve-seconds", type=float, default=0.5, help="arrival span per rate")
+    p.add_argument("--serve-seconds", type=float, default=1.0, help="arrival span per rate")
     p.add_argument("--serve-evict-frac", type=float, default=0.5,
                    help="scene memory budget of the eviction measurement, as a fraction of the scenes' footprint")
     p.add_argument("--cpu-budget-s", type=float, default=20.0, help="CPU-baseline sample budget")
@@ -596,7 +596,9 @@ def run_serving(args):
     cfg = Configuration(depth_sorting=DepthSorting.GPU, use_covariance_for_scale=True, use_unaligned_rectangles=True,
                         spherical_harmonics_order=3, max_splat_count=max(sizes),
                         field_of_view_y=math.radians(60.0), blend_mode=BlendMode.UNORM8)
-    warm = _serve_requests(args.serve_requests // 2, seed=args.seed + 31, n_scenes=len(sizes))
+    # long enough that every slot has met every (viewport, scene-size class) pair it will see, so that
+    # graph captures fall into the warm-up
+    warm = _serve_requests(3 * args.serve_requests // 2, seed=args.seed + 31, n_scenes=len(sizes))
     closed = _serve_requests(args.serve_requests, seed=args.seed + 37, n_scenes=len(sizes))
     rates = [float(x) for x in args.serve_rates.split(",") if x]
     out = {"workload": SERVE_WORKLOAD, "scenes": len(sizes), "scene_splats": sizes,

@@ -109,9 +109,14 @@ static int ensure_ranges(spl_renderer* r, uint64_t tiles) {
     cudaError_t e = cudaDeviceSynchronize();  // the old buffer may still be read by a frame in flight
     if (e != cudaSuccess) return fail(SPL_ERR_CUDA, "ranges resize: %s", cudaGetErrorString(e));
     dfree(r->ranges);
+    dfree(r->tile_order);
     r->ranges_cap = 0;
     int rc = dalloc(&r->ranges, tiles);
-    if (rc) return rc;
+    if (!rc) rc = dalloc(&r->tile_order, tiles);
+    if (rc) {
+        dfree(r->ranges);
+        return rc;
+    }
     r->ranges_cap = tiles;
     return SPL_OK;
 }
@@ -356,7 +361,8 @@ static int render_frame_impl(spl_renderer* r, const SceneView& sv, const Uniform
     r->mark(5, st);
     launch_tile_ranges(pk, r->fc, (uint32_t)r->pair_cap, r->ranges, st);
     r->mark(6, st);
-    launch_raster(cfg.use_unaligned_rectangles != 0, cfg.blend_mode, r->ranges, pv, r->rec, u, out_device, st);
+    launch_raster(cfg.use_unaligned_rectangles != 0, cfg.blend_mode, r->ranges, r->order_tiles ? r->tile_order : nullptr,
+                  pv, r->rec, u, out_device, st);
     r->mark(7, st);
     CU(cudaGetLastError());
     r->final_pair_vals = pv;
@@ -439,8 +445,9 @@ int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint3
     const bool coop = r->sort_mode == SPL_SORT_COOPERATIVE;
     const int depth_sort = r->cfg.depth_sorting == DS_NONE ? 0 : (coop ? 1 : 4);
     // frame_begin, cull, preprocess, depth sort (one cooperative launch or 4 onesweep passes),
-    // ranges memset, bin, pair sort (one cooperative launch or one launch per pass), ranges, raster
-    return 1 + 1 + 1 + depth_sort + 1 + 1 + (coop ? 1 : pair_passes) + 1 + 1;
+    // ranges memset, bin, pair sort (one cooperative launch or one launch per pass), ranges, tile
+    // order, raster
+    return 1 + 1 + 1 + depth_sort + 1 + 1 + (coop ? 1 : pair_passes) + 1 + (r->order_tiles ? 1 : 0) + 1;
 }
 
 int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,

@@ -8,6 +8,7 @@
 //                    load-balanced emission inside the CTA and the tile-id digit histograms
 //   (2 onesweep passes over the 16-bit tile ids: stable, so each tile's list stays in depth order)
 //   k_tile_ranges  - start/end of each tile's run in the sorted pair list
+//   k_tile_order   - the raster's tile order: most pairs first
 //   k_raster       - one CTA per tile, one thread per pixel; records staged through shared memory in
 //                    batches of 256, warp-uniform box rejection, exact coverage test, falloff, blend,
 //                    and early exit once every pixel of the tile is opaque
@@ -159,6 +160,69 @@ void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint
 }
 
 // ------------------------------------------------------------------------------------------------
+// The raster's tile order: tiles with more (tile, splat) pairs first, in buckets of half an octave of
+// the pair count (2 buckets per power of two), empty tiles last.  Tiles take very different times
+// (dense clusters against open sky); started in row-major order, a few heavy tiles could begin in
+// the last wave and set the kernel's end, while heavy-first is close to the longest-processing-time
+// schedule.  Tiles are independent, so the order changes no pixel.  One CTA: a bucket histogram, its
+// scan and a scatter of tile indices (the order within a bucket does not matter).
+constexpr int ORDER_BUCKETS = 65;
+
+__device__ __forceinline__ uint32_t order_bucket(uint2 r) {
+    const uint32_t c = r.y - r.x;
+    if (c == 0u) return ORDER_BUCKETS - 1;
+    const uint32_t l = 31u - __clz(c);                     // floor(log2 c)
+    const uint32_t half = l > 0u ? (c >> (l - 1u)) & 1u : 0u;  // the bit after the leading one
+    return 63u - (2u * l + half);                          // more pairs -> smaller bucket
+}
+
+constexpr uint32_t ORDER_SMEM_TILES = 32768;  // tiles whose bucket is kept in shared memory (2160p: 32,400)
+
+__global__ void __launch_bounds__(1024) k_tile_order(const uint2* __restrict__ ranges, uint32_t ntiles,
+                                                     uint32_t* __restrict__ order) {
+    __shared__ uint32_t cnt[ORDER_BUCKETS];
+    __shared__ uint8_t bkt[ORDER_SMEM_TILES];
+    const uint32_t lane = threadIdx.x & 31u;
+    if (threadIdx.x < ORDER_BUCKETS) cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    // histogram; lanes of a warp with the same bucket add once (most tiles share a few buckets)
+#pragma unroll 4
+    for (uint32_t t = threadIdx.x; t < ntiles; t += blockDim.x) {
+        const uint32_t b = order_bucket(__ldg(ranges + t));
+        if (t < ORDER_SMEM_TILES) bkt[t] = (uint8_t)b;
+        const uint32_t peers = __match_any_sync(__activemask(), b);
+        if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&cnt[b], __popc(peers));
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive scan of the 65 bucket counts by one warp
+        uint32_t carry = 0;
+        for (int b0 = 0; b0 < ORDER_BUCKETS; b0 += 32) {
+            const int b = b0 + (int)threadIdx.x;
+            const uint32_t v = b < ORDER_BUCKETS ? cnt[b] : 0u;
+            uint32_t x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
+                if ((int)threadIdx.x >= o) x += y;
+            }
+            if (b < ORDER_BUCKETS) cnt[b] = carry + x - v;
+            carry += __shfl_sync(FULL_MASK, x, 31);
+        }
+    }
+    __syncthreads();
+    // scatter: one atomic per (warp, bucket), lanes take consecutive places in lane order
+    for (uint32_t t = threadIdx.x; t < ntiles; t += blockDim.x) {
+        const uint32_t b = t < ORDER_SMEM_TILES ? bkt[t] : order_bucket(__ldg(ranges + t));
+        const uint32_t peers = __match_any_sync(__activemask(), b);
+        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&cnt[b], __popc(peers));
+        base = __shfl_sync(peers, base, (int)leader);
+        order[base + __popc(peers & lanemask_lt())] = t;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
 constexpr int RASTER_BATCH = 256;
 
 // One CTA per 16x16 tile, one thread per pixel.  Warp w owns rows 2w, 2w+1, split into eight 2x2-pixel
@@ -190,7 +254,8 @@ __device__ __forceinline__ void g_interval(float c, float s, float T, int& lo, i
 }
 
 template <bool RECT, int BLEND>
-__global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ pair_vals,
+__global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ tile_order,
+                                                const uint32_t* __restrict__ pair_vals,
                                                 const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
                                                 float psx, float psy, void* __restrict__ out) {
     __shared__ float4 s_q0[RASTER_BATCH], s_q1[RASTER_BATCH], s_q2[RASTER_BATCH];
@@ -198,7 +263,7 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     __shared__ float s_lut[256];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     const uint32_t grp = lane >> 2, li = lane & 3u;
-    const int tile = blockIdx.x;
+    const int tile = tile_order ? (int)__ldg(tile_order + blockIdx.x) : (int)blockIdx.x;
     const int tx = tile % tiles_x, ty = tile / tiles_x;
     const int bx0 = tx * TILE_PIXELS + 2 * (int)grp;  // this lane's 2x2 block
     const int by0 = ty * TILE_PIXELS + 2 * (int)w;
@@ -335,24 +400,26 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
     }
 }
 
-void launch_raster(bool rect, int blend, const uint2* ranges, const uint32_t* pair_vals, const float4* rec,
-                   const Uniforms& u, void* out, cudaStream_t st) {
+void launch_raster(bool rect, int blend, const uint2* ranges, uint32_t* tile_order, const uint32_t* pair_vals,
+                   const float4* rec, const Uniforms& u, void* out, cudaStream_t st) {
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];
     const int tiles_x = (W + TILE_PIXELS - 1) / TILE_PIXELS, tiles_y = (H + TILE_PIXELS - 1) / TILE_PIXELS;
     const int grid = tiles_x * tiles_y;
     if (grid == 0) return;
     const float psx = (2.0f * u.view_size[0]) / (float)W;
     const float psy = -((2.0f * u.view_size[1]) / (float)H);
+    if (tile_order) k_tile_order<<<1, 1024, 0, st>>>(ranges, (uint32_t)grid, tile_order);
+    const uint32_t* o = tile_order;
     if (rect) {
         if (blend == 0)
-            k_raster<true, 0><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+            k_raster<true, 0><<<grid, 256, 0, st>>>(ranges, o, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
         else
-            k_raster<true, 1><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+            k_raster<true, 1><<<grid, 256, 0, st>>>(ranges, o, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
     } else {
         if (blend == 0)
-            k_raster<false, 0><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+            k_raster<false, 0><<<grid, 256, 0, st>>>(ranges, o, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
         else
-            k_raster<false, 1><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
+            k_raster<false, 1><<<grid, 256, 0, st>>>(ranges, o, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy, out);
     }
 }
 

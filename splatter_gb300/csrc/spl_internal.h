@@ -88,6 +88,8 @@ struct spl_renderer {
     uint64_t* st_pairs = nullptr;      // onesweep mode: look-back status of the <= 3 pair passes
     FrameCounters* host_fc = nullptr;  // pinned
     uint2* ranges = nullptr;
+    uint32_t* tile_order = nullptr;  // the raster's tile order, most pairs first (ranges_cap entries)
+    bool order_tiles = true;         // off where concurrent frames already hide the raster's tail (serving)
     uint64_t ranges_cap = 0;
     // last frame
     cudaStream_t last_stream = nullptr;
@@ -107,7 +109,7 @@ struct spl_renderer {
         dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes); dfree(grad_rec);
         dfree(st_cull); dfree(st_bin);
         dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b);
-        dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges); dfree(d_u); dfree(d_sv);
+        dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges); dfree(tile_order); dfree(d_u); dfree(d_sv);
         dfree(st_sort); dfree(st_pairs);
         if (host_fc) cudaFreeHost(host_fc);
         host_fc = nullptr;

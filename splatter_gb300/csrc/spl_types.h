@@ -92,8 +92,10 @@ void launch_bin(int mode, const uint32_t* order, const uint2* boxes, FrameCounte
                 uint32_t max_n, uint32_t spin_limit, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint32_t pair_cap, uint2* ranges,
                         cudaStream_t st);
-void launch_raster(bool rect, int blend, const uint2* ranges, const uint32_t* pair_vals, const float4* rec,
-                   const Uniforms& u, void* out, cudaStream_t st);
+// Orders the tiles most pairs first (tile_order, one entry per tile), then rasterises them in that order;
+// with tile_order == nullptr in row-major order.
+void launch_raster(bool rect, int blend, const uint2* ranges, uint32_t* tile_order, const uint32_t* pair_vals,
+                   const float4* rec, const Uniforms& u, void* out, cudaStream_t st);
 void launch_load_records(const float* records62, uint32_t count, float* x, float* y, float* z, float4* rot,
                          float4* scale_alpha, float* sh, cudaStream_t st);
 void launch_splats60_to_soa(const float* s60, uint32_t count, float* x, float* y, float* z, float4* rot,

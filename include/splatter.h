@@ -183,6 +183,23 @@ SPL_API int spl_render_backward(spl_renderer* r, const spl_scene* scene, const f
                                 const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z,
                                 float* grad_rotation, float* grad_scale_alpha, float* grad_sh, void* stream);
 
+/* The loader's activations (Scene::load_chunk, scene.rs:225-250) on device arrays of raw parameters,
+ * for training: means (n x 3), quaternions (n x 4, scalar first), log-scales (n x 3) and opacity
+ * logits (n) -> the arrays of a wrapped scene (x, y, z planes; unit rotations n x 4; scale + opacity
+ * n x 4).  The arithmetic is the loader's, so a frame of these arrays equals the frame of a scene
+ * loaded from the same file records.  Asynchronous on `stream`. */
+SPL_API int spl_activate_splats(uint64_t n, const float* means, const float* quaternions, const float* log_scales,
+                                const float* opacity_logits, float* x, float* y, float* z, float* rotation,
+                                float* scale_alpha, void* stream);
+/* Its backward: gradients of the activated arrays (x, y, z planes, rotation, scale_alpha) -> gradients
+ * of the raw parameters (written, not accumulated).  Needs the raw quaternions and log-scales and the
+ * activated rotation and scale_alpha. */
+SPL_API int spl_activate_splats_backward(uint64_t n, const float* quaternions, const float* log_scales,
+                                         const float* rotation, const float* scale_alpha, const float* grad_x,
+                                         const float* grad_y, const float* grad_z, const float* grad_rotation,
+                                         const float* grad_scale_alpha, float* grad_means, float* grad_quaternions,
+                                         float* grad_log_scales, float* grad_opacity_logits, void* stream);
+
 /* Copies the last backward pass's per-record gradients (10 floats per visible splat, compaction
  * order: d/dA00, d/dA01, d/dB0, d/dA10, d/dA11, d/dB1 with A taken against pixel offsets from the
  * centre of the record's pixel box and B at that centre, then d/dopacity, d/dr, d/dg, d/db) into a

@@ -145,6 +145,8 @@ SIGNATURES = [
     ("spl_server_poll", I32, [P, ctypes.POINTER(SplCompletion), U32, ctypes.POINTER(U32), ctypes.c_int64]),
     ("spl_server_get_stats", I32, [P, ctypes.POINTER(SplServerStats)]),
     ("spl_server_now_ns", U64, []),
+    ("spl_activate_splats", I32, [U64, P, P, P, P, P, P, P, P, P, P]),
+    ("spl_activate_splats_backward", I32, [U64, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
 ]
 
 NO_ALLOC_MAX_PAIRS = 262144

@@ -4,8 +4,10 @@
 opacities, SH) and returns the float4 image of an fp32-blend frame; its backward calls
 spl_render_backward (raster backward + vertex-stage backward on the GPU).  `render_raw` applies the
 file loader's activations first (Scene::load_chunk, scene.rs:225-250: rotor normalisation, exp of the
-log-scales clamped to mean +- 5, sigmoid of the opacity logit), so gradients reach the raw
-parameters a training loop optimises.  Depth order, culling and the 1/255 discard are constants of
+log-scales clamped to mean +- 5, sigmoid of the opacity logit) with the loader's own arithmetic on the
+GPU (spl_activate_splats) and chains its backward there too (spl_activate_splats_backward), so
+gradients reach the raw parameters a training loop optimises without torch elementwise kernels per
+frame.  `activate` is the same transform written in torch (a reference).  Depth order, culling and the 1/255 discard are constants of
 the frame (no gradient), as in any splat rasteriser.
 """
 import ctypes
@@ -16,7 +18,7 @@ from . import _lib
 from ._lib import check
 from .renderer import BlendMode, Renderer, _stream_ptr
 
-__all__ = ["render_splats", "render_raw", "activate"]
+__all__ = ["render_splats", "render_raw", "activate", "activate_native"]
 
 
 def _ptr(t):
@@ -84,13 +86,8 @@ class _RenderSplats:  # built lazily so that importing the package does not impo
                 @staticmethod
                 def backward(ctx, grad_img):
                     (img,) = ctx.saved_tensors
+                    _frame_ready(ctx)
                     r = ctx.renderer
-                    w, h = ctx.size
-                    key = (id(ctx.scene), ctx.cam.tobytes(), w, h)
-                    if getattr(r, "_last_frame_key", None) != key:
-                        # another frame was rendered since: re-render this one (deterministic)
-                        r.render_frame(ctx.scene, ctx.cam, w, h)
-                        r._last_frame_key = key
                     xyz, rot, sa, sh = ctx.scene._keep
                     gxyz = torch.zeros_like(xyz)
                     grot = torch.zeros_like(rot)
@@ -106,12 +103,99 @@ class _RenderSplats:  # built lazily so that importing the package does not impo
         return cls.fn
 
 
+def _frame_ready(ctx):
+    """Re-renders the frame of this autograd node if the renderer has rendered another one since."""
+    r = ctx.renderer
+    w, h = ctx.size
+    key = (id(ctx.scene), ctx.cam.tobytes(), w, h)
+    if getattr(r, "_last_frame_key", None) != key:
+        r.render_frame(ctx.scene, ctx.cam, w, h)  # deterministic: the same frame again
+        r._last_frame_key = key
+
+
+class _RenderRaw:  # built lazily, like _RenderSplats
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is None:
+            torch = _import_torch()
+
+            class RenderRaw(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, means, quats, log_scales, logits, sh, renderer, camera_to_world, width, height):
+                    means, quats, log_scales, logits, sh = (t.contiguous() for t in (means, quats, log_scales, logits,
+                                                                                      sh))
+                    n = quats.shape[0]
+                    f32 = dict(device=quats.device, dtype=torch.float32)
+                    xyz = torch.empty((3, n), **f32)
+                    rot = torch.empty((n, 4), **f32)
+                    sa = torch.empty((n, 4), **f32)
+                    lib = _lib.load()
+                    check(lib.spl_activate_splats(n, _ptr(means), _ptr(quats), _ptr(log_scales), _ptr(logits),
+                                                  _ptr(xyz[0]), _ptr(xyz[1]), _ptr(xyz[2]), _ptr(rot), _ptr(sa),
+                                                  _stream_ptr(None)))
+                    scene = _WrappedScene(renderer, xyz, rot, sa, sh)
+                    img = renderer.render_frame(scene, camera_to_world, width, height)
+                    ctx.renderer = renderer
+                    ctx.scene = scene
+                    ctx.cam = np.ascontiguousarray(np.asarray(camera_to_world, np.float32).reshape(16))
+                    ctx.size = (width, height)
+                    ctx.save_for_backward(img, quats, log_scales)
+                    renderer._last_frame_key = (id(scene), ctx.cam.tobytes(), width, height)
+                    return img
+
+                @staticmethod
+                def backward(ctx, grad_img):
+                    img, quats, log_scales = ctx.saved_tensors
+                    _frame_ready(ctx)
+                    r = ctx.renderer
+                    xyz, rot, sa, sh = ctx.scene._keep
+                    n = rot.shape[0]
+                    gxyz = torch.zeros_like(xyz)
+                    grot = torch.zeros_like(rot)
+                    gsa = torch.zeros_like(sa)
+                    gsh = torch.zeros_like(sh)
+                    g = grad_img.contiguous().float()
+                    st = _stream_ptr(None)
+                    check(r._lib.spl_render_backward(r.handle, ctx.scene.handle, _ptr(img), _ptr(g), _ptr(gxyz[0]),
+                                                     _ptr(gxyz[1]), _ptr(gxyz[2]), _ptr(grot), _ptr(gsa), _ptr(gsh),
+                                                     st))
+                    g_means = torch.empty((n, 3), device=rot.device, dtype=torch.float32)
+                    g_quats = torch.empty((n, 4), device=rot.device, dtype=torch.float32)
+                    g_logs = torch.empty((n, 3), device=rot.device, dtype=torch.float32)
+                    g_logits = torch.empty((n,), device=rot.device, dtype=torch.float32)
+                    check(r._lib.spl_activate_splats_backward(n, _ptr(quats), _ptr(log_scales), _ptr(rot), _ptr(sa),
+                                                              _ptr(gxyz[0]), _ptr(gxyz[1]), _ptr(gxyz[2]),
+                                                              _ptr(grot), _ptr(gsa), _ptr(g_means), _ptr(g_quats),
+                                                              _ptr(g_logs), _ptr(g_logits), st))
+                    return g_means, g_quats, g_logs, g_logits, gsh, None, None, None, None
+
+            cls.fn = RenderRaw
+        return cls.fn
+
+
 def render_splats(xyz, rotation, scale_alpha, sh, renderer: Renderer, camera_to_world, width, height):
     """Differentiable frame.  xyz: (3, N) centre planes; rotation: (N, 4) scalar first; scale_alpha:
     (N, 4) scale xyz + opacity; sh: (N, 48).  Returns (H, W, 4) float32 (r, g, b, T)."""
     if renderer.config.blend_mode != BlendMode.FP32:
         raise ValueError("render_splats needs a renderer with blend_mode FP32")
     return _RenderSplats.get().apply(xyz, rotation, scale_alpha, sh, renderer, camera_to_world, width, height)
+
+
+def activate_native(means, quats, log_scales, opacity_logits):
+    """The loader's activations on the GPU (spl_activate_splats, no autograd): (xyz planes (3, N),
+    rotation (N, 4), scale_alpha (N, 4)), bit for bit the arrays of a scene loaded from records."""
+    torch = _import_torch()
+    means, quats, log_scales, opacity_logits = (t.detach().contiguous() for t in (means, quats, log_scales,
+                                                                                  opacity_logits))
+    n = quats.shape[0]
+    f32 = dict(device=quats.device, dtype=torch.float32)
+    xyz, rot, sa = torch.empty((3, n), **f32), torch.empty((n, 4), **f32), torch.empty((n, 4), **f32)
+    check(_lib.load().spl_activate_splats(n, _ptr(means), _ptr(quats), _ptr(log_scales), _ptr(opacity_logits),
+                                          _ptr(xyz[0]), _ptr(xyz[1]), _ptr(xyz[2]), _ptr(rot), _ptr(sa),
+                                          _stream_ptr(None)))
+    return xyz, rot, sa
 
 
 def activate(means, quats, log_scales, opacity_logits):
@@ -126,6 +210,13 @@ def activate(means, quats, log_scales, opacity_logits):
 
 
 def render_raw(means, quats, log_scales, opacity_logits, sh, renderer, camera_to_world, width, height):
-    """Differentiable frame from raw parameters (positions, quaternions, log-scales, opacity logits, SH)."""
-    xyz, rot, sa = activate(means, quats, log_scales, opacity_logits)
-    return render_splats(xyz, rot, sa, sh, renderer, camera_to_world, width, height)
+    """Differentiable frame from raw parameters: means (N, 3), quaternions (N, 4, scalar first),
+    log-scales (N, 3), opacity logits (N,), SH (N, 48), all float32 CUDA tensors.  The frame equals the
+    frame of a scene loaded from the same file records; gradients reach every raw parameter."""
+    if renderer.config.blend_mode != BlendMode.FP32:
+        raise ValueError("render_raw needs a renderer with blend_mode FP32")
+    for t, shape in ((means, 3), (quats, 4), (log_scales, 3), (sh, 48)):
+        if t.dim() != 2 or t.shape[1] != shape or t.dtype.itemsize != 4 or not t.is_cuda:
+            raise ValueError("render_raw: float32 CUDA tensors (N, 3), (N, 4), (N, 3), (N,), (N, 48) expected")
+    return _RenderRaw.get().apply(means, quats, log_scales, opacity_logits, sh, renderer, camera_to_world, width,
+                                  height)

@@ -467,7 +467,7 @@ int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* im
     const spl_config& cfg = r->cfg;
     launch_backward((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
                     cfg.use_unaligned_rectangles != 0, scene->view(), r->last_u, r->idx, r->fc, r->boxes, r->ranges,
-                    r->final_pair_vals, r->rec, reinterpret_cast<const float4*>(image_device),
+                    r->order_tiles ? r->tile_order : nullptr, r->final_pair_vals, r->rec, reinterpret_cast<const float4*>(image_device),
                     reinterpret_cast<const float4*>(grad_image_device), r->grad_rec, (uint32_t)scene->n, grad_x,
                     grad_y, grad_z, reinterpret_cast<float4*>(grad_rotation), reinterpret_cast<float4*>(grad_scale_alpha),
                     grad_sh, st);
@@ -919,6 +919,36 @@ int spl_scene_load_chunk_device(spl_scene* s, const float* records_device, uint6
         launch_load_records(records_device + first * 62, (uint32_t)cnt, s->x + at, s->y + at, s->z + at, s->rot + at,
                             s->scale_alpha + at, s->sh + at * 48, (cudaStream_t)stream);
     }
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
+int spl_activate_splats(uint64_t n, const float* means, const float* quaternions, const float* log_scales,
+                        const float* opacity_logits, float* x, float* y, float* z, float* rotation, float* scale_alpha,
+                        void* stream) {
+    if (n == 0) return SPL_OK;
+    if (!means || !quaternions || !log_scales || !opacity_logits || !x || !y || !z || !rotation || !scale_alpha)
+        return fail(SPL_ERR_INVALID, "NULL argument");
+    if (n > MAX_COUNT) return fail(SPL_ERR_INVALID, "%llu splats", (unsigned long long)n);
+    launch_activate((uint32_t)n, means, quaternions, log_scales, opacity_logits, x, y, z, rotation, scale_alpha,
+                    (cudaStream_t)stream);
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
+int spl_activate_splats_backward(uint64_t n, const float* quaternions, const float* log_scales, const float* rotation,
+                                 const float* scale_alpha, const float* grad_x, const float* grad_y,
+                                 const float* grad_z, const float* grad_rotation, const float* grad_scale_alpha,
+                                 float* grad_means, float* grad_quaternions, float* grad_log_scales,
+                                 float* grad_opacity_logits, void* stream) {
+    if (n == 0) return SPL_OK;
+    if (!quaternions || !log_scales || !rotation || !scale_alpha || !grad_x || !grad_y || !grad_z || !grad_rotation ||
+        !grad_scale_alpha || !grad_means || !grad_quaternions || !grad_log_scales || !grad_opacity_logits)
+        return fail(SPL_ERR_INVALID, "NULL argument");
+    if (n > MAX_COUNT) return fail(SPL_ERR_INVALID, "%llu splats", (unsigned long long)n);
+    launch_activate_backward((uint32_t)n, quaternions, log_scales, rotation, scale_alpha, grad_x, grad_y, grad_z,
+                             grad_rotation, grad_scale_alpha, grad_means, grad_quaternions, grad_log_scales,
+                             grad_opacity_logits, (cudaStream_t)stream);
     CU(cudaGetLastError());
     return SPL_OK;
 }

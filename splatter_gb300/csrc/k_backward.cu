@@ -33,6 +33,7 @@ __global__ void k_zero_grad_rec(float* grad_rec, const FrameCounters* fc) {
 
 template <bool RECT>
 __global__ void __launch_bounds__(256) k_raster_backward(const uint2* __restrict__ ranges,
+                                                         const uint32_t* __restrict__ tile_order,
                                                          const uint32_t* __restrict__ pair_vals,
                                                          const float4* __restrict__ rec, int W, int H, int tiles_x,
                                                          float margin, float psx, float psy,
@@ -44,7 +45,8 @@ __global__ void __launch_bounds__(256) k_raster_backward(const uint2* __restrict
     __shared__ uint32_t s_slot[256];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     const uint32_t grp = lane >> 3, li = lane & 7u;
-    const int tile = blockIdx.x;
+    // the forward's most-pairs-first order of this frame's tiles, when it made one
+    const int tile = tile_order ? (int)__ldg(tile_order + blockIdx.x) : (int)blockIdx.x;
     const int tx = tile % tiles_x, ty = tile / tiles_x;
     const int bx0 = tx * TILE_PIXELS + 4 * (int)grp;
     const int by0 = ty * TILE_PIXELS + 2 * (int)w;
@@ -273,8 +275,8 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
 
 void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
                      const uint32_t* idx, const FrameCounters* fc, const uint2* boxes, const uint2* ranges,
-                     const uint32_t* pair_vals,
-                     const float4* rec, const float4* image, const float4* grad_image, float* grad_rec,
+                     const uint32_t* tile_order, const uint32_t* pair_vals, const float4* rec, const float4* image,
+                     const float4* grad_image, float* grad_rec,
                      uint32_t max_n, float* gx, float* gy, float* gz, float4* grot, float4* gscale_alpha, float* gsh,
                      cudaStream_t st) {
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];
@@ -288,11 +290,11 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
     const int grid = tiles_x * tiles_y;
     if (grid > 0) {
         if (rect)
-            k_raster_backward<true><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx, psy,
-                                                          image, grad_image, grad_rec);
+            k_raster_backward<true><<<grid, 256, 0, st>>>(ranges, tile_order, pair_vals, rec, W, H, tiles_x, u.margin,
+                                                          psx, psy, image, grad_image, grad_rec);
         else
-            k_raster_backward<false><<<grid, 256, 0, st>>>(ranges, pair_vals, rec, W, H, tiles_x, u.margin, psx,
-                                                           psy, image, grad_image, grad_rec);
+            k_raster_backward<false><<<grid, 256, 0, st>>>(ranges, tile_order, pair_vals, rec, W, H, tiles_x,
+                                                           u.margin, psx, psy, image, grad_image, grad_rec);
     }
     if (max_n == 0) return;
     uint32_t blocks = (max_n + 127) / 128;

@@ -332,19 +332,13 @@ __global__ void __launch_bounds__(LOAD_BLOCK) k_load_records(const float* __rest
     if (t < nrec) {
         const float* r = s_buf + t * 62u;
         const uint32_t i = first + t;
-        const float q0 = r[58], q1 = r[59], q2 = r[60], q3 = r[61];
-        const float inv = 1.0f / sqrtf(((q0 * q0 + q1 * q1) + q2 * q2) + q3 * q3);
-        rot[i] = make_float4(q0 * inv, q1 * inv, q2 * inv, q3 * inv);
+        float4 q, sa;
+        activate_splat(r[58], r[59], r[60], r[61], r[55], r[56], r[57], r[54], q, sa);
+        rot[i] = q;
+        scale_alpha[i] = sa;
         x[i] = r[0];
         y[i] = r[1];
         z[i] = r[2];
-        const float avg = ((r[55] + r[56]) + r[57]) / 3.0f;
-        const float lo = avg - 5.0f, hi = avg + 5.0f;
-        const float s0 = spl_expf(fminf(fmaxf(r[55], lo), hi));
-        const float s1 = spl_expf(fminf(fmaxf(r[56], lo), hi));
-        const float s2 = spl_expf(fminf(fmaxf(r[57], lo), hi));
-        const float a = 1.0f / (1.0f + spl_expf(-r[54]));
-        scale_alpha[i] = make_float4(s0, s1, s2, a);
     }
     float* dst = sh + (size_t)first * 48u;
     for (uint32_t k = threadIdx.x; k < nrec * 48u; k += LOAD_BLOCK) {

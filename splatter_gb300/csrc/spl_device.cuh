@@ -150,6 +150,21 @@ __device__ __forceinline__ float spl_expf_nonpos(float x) {
     return __fmul_rn(p, __int_as_float(((int)n + 127) << 23));
 }
 
+// The loader's transform of one splat (Scene::load_chunk, scene.rs:225-250): quaternion normalised,
+// log-scales clamped to their mean +- 5 and exponentiated, opacity logit through the sigmoid.
+__device__ __forceinline__ void activate_splat(float q0, float q1, float q2, float q3, float l0, float l1, float l2,
+                                               float logit, float4& rot, float4& scale_alpha) {
+    const float inv = 1.0f / sqrtf(((q0 * q0 + q1 * q1) + q2 * q2) + q3 * q3);
+    rot = make_float4(q0 * inv, q1 * inv, q2 * inv, q3 * inv);
+    const float avg = ((l0 + l1) + l2) / 3.0f;
+    const float lo = avg - 5.0f, hi = avg + 5.0f;
+    const float s0 = spl_expf(fminf(fmaxf(l0, lo), hi));
+    const float s1 = spl_expf(fminf(fmaxf(l1, lo), hi));
+    const float s2 = spl_expf(fminf(fmaxf(l2, lo), hi));
+    const float a = 1.0f / (1.0f + spl_expf(-logit));
+    scale_alpha = make_float4(s0, s1, s2, a);
+}
+
 __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 
 // WGSL u32(f32): truncate, saturate, NaN -> 0.

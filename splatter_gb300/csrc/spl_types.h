@@ -109,11 +109,19 @@ cudaError_t launch_sort_coop(uint32_t* keys0, uint32_t* keys1, uint32_t* vals0, 
                              const uint32_t* n_ptr, uint32_t n_cap, int passes, int shift0, uint32_t* cnt,
                              uint32_t* bar, uint32_t spin_limit, uint32_t* err, cudaStream_t st);
 int sort_coop_grid();
+// The loader's activations of raw parameters and their backward (k_activate.cu).
+void launch_activate(uint32_t n, const float* means, const float* quats, const float* logs, const float* logits,
+                     float* x, float* y, float* z, float* rot, float* scale_alpha, cudaStream_t st);
+void launch_activate_backward(uint32_t n, const float* quats, const float* logs, const float* rot,
+                              const float* scale_alpha, const float* gx, const float* gy, const float* gz,
+                              const float* grot, const float* gsa, float* g_means, float* g_quats, float* g_logs,
+                              float* g_logits, cudaStream_t st);
 // Backward of the last frame (fp32 blend): raster backward into grad_rec (10 floats per record),
 // then the vertex-stage backward into per-splat parameter gradients.
 void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
                      const uint32_t* idx, const FrameCounters* fc, const uint2* boxes, const uint2* ranges,
-                     const uint32_t* pair_vals, const float4* rec, const float4* image, const float4* grad_image,
+                     const uint32_t* tile_order, const uint32_t* pair_vals, const float4* rec, const float4* image,
+                     const float4* grad_image,
                      float* grad_rec,
                      uint32_t max_n, float* gx, float* gy, float* gz, float4* grot, float4* gscale_alpha, float* gsh,
                      cudaStream_t st);

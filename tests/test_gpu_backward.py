@@ -29,7 +29,7 @@ import numpy as np
 import pytest
 
 import oracle
-from splatter_gb300 import BlendMode, Configuration, Renderer, camera, synthetic
+from splatter_gb300 import BlendMode, Configuration, Renderer, Scene, camera, synthetic
 from splatter_gb300.autograd import render_raw, render_splats
 
 pytestmark = pytest.mark.gpu
@@ -235,46 +235,44 @@ def test_parameter_gradients_match_finite_differences(frame):
 
 
 def test_raw_parameter_gradients_through_autograd(cuda):
-    """render_raw: the loader's activations in torch + the hand-written backward; the chain matches
-    the activated-parameter gradients pushed through the analytic activation Jacobians."""
+    """render_raw: the loader's activations and their backward on the GPU around the hand-written
+    backward.  The frame equals the frame of a scene loaded from the same file records, and the raw
+    gradients equal torch autograd's vector-Jacobian product through the torch restatement of the
+    activations (`activate`) applied to the activated-parameter gradients of the same frame.  Some
+    splats have a log-scale beyond mean + 5, so the clamp (whose gradient goes through the mean of
+    all three) is exercised."""
     import torch
+    from splatter_gb300.autograd import activate, activate_native
     n, W, H = 5000, 128, 96
     rec, cam, cfg = _setup(n, W, H, seed=51, scale_boost=1.0)
+    rec[::250, 57] = rec[::250, 55] + 8.0  # clamped to mean + 5
     r = Renderer(cfg)
-    means = torch.tensor(rec[:, 0:3], device="cuda", requires_grad=True)
-    quats = torch.tensor(rec[:, 58:62], device="cuda", requires_grad=True)
-    logs = torch.tensor(rec[:, 55:58], device="cuda", requires_grad=True)
-    logits = torch.tensor(rec[:, 54], device="cuda", requires_grad=True)
-    sh = torch.tensor(rec[:, 6:54], device="cuda", requires_grad=True)
+    leaves = [torch.tensor(rec[:, a:b], device="cuda").squeeze(1).contiguous().requires_grad_(True)
+              for a, b in ((0, 3), (58, 62), (55, 58), (54, 55), (6, 54))]
+    means, quats, logs, logits, sh = leaves
     img = render_raw(means, quats, logs, logits, sh, r, cam, W, H)
-    loss = (img[..., :3] ** 2).sum()
-    loss.backward()
-    # activated gradients of the same frame
-    with torch.no_grad():
-        q = quats.detach()
-        nq = torch.sqrt((q * q).sum(-1, keepdim=True))
-        rot = q * (1.0 / nq)
-        scale = torch.exp(logs.detach())
-        alpha = torch.sigmoid(logits.detach())
-    xyz = means.detach().t().contiguous().requires_grad_(True)
-    rot_ = rot.clone().requires_grad_(True)
-    sa_ = torch.cat([scale, alpha[:, None]], 1).requires_grad_(True)
+    (img[..., :3] ** 2).sum().backward()
+    # the same frame from records through the loader
+    sc = Scene(r, n)
+    sc.load_chunk(rec)
+    assert torch.equal(img, r.render_frame(sc, cam, W, H))
+    # activated gradients of the same frame (same activated values, bit for bit)
+    xyz, rot, sa = activate_native(means, quats, logs, logits)
+    act = [t.clone().requires_grad_(True) for t in (xyz, rot, sa)]
     sh_ = sh.detach().clone().requires_grad_(True)
-    img2 = render_splats(xyz, rot_, sa_, sh_, r, cam, W, H)
+    img2 = render_splats(act[0], act[1], act[2], sh_, r, cam, W, H)
     assert torch.equal(img, img2)
     (img2[..., :3] ** 2).sum().backward()
+    # chain through the torch restatement of the activations
+    raw = [t.detach().clone().requires_grad_(True) for t in (means, quats, logs, logits)]
+    ref = torch.autograd.grad(activate(*raw), raw, grad_outputs=[a.grad for a in act])
     torch.cuda.synchronize()
     # float atomics make the gradient sums order-dependent: compare at 1e-4 of each array's scale
     def close(a, b):
         return torch.allclose(a, b, rtol=1e-4, atol=1e-4 * float(b.abs().max()))
-    assert close(means.grad, xyz.grad.t())
     assert close(sh.grad, sh_.grad)
-    # log-scale: d scale / d log-scale = scale;  logit: d alpha / d logit = alpha (1 - alpha)
-    assert close(logs.grad, sa_.grad[:, :3] * scale)
-    assert close(logits.grad, sa_.grad[:, 3] * alpha * (1 - alpha))
-    # quaternion: projection of the rotation gradient onto the tangent space, divided by |q|
-    gq = (rot_.grad - (rot_.grad * rot).sum(-1, keepdim=True) * rot) / nq
-    assert close(quats.grad, gq)
+    for got, want in zip((means.grad, quats.grad, logs.grad, logits.grad), ref):
+        assert close(got, want)
 
 
 def test_backward_requires_fp32_blend(cuda):

@@ -73,6 +73,32 @@ def dist_info():
     return rank, world, local
 
 
+def reduce_max(x, device="cuda"):
+    """Max over the ranks of the job (one process per GPU); the identity for a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, ms_max):
+    """Whole-job rate: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / (ms_max / 1000.0)
+
+
+def bench_config(args, world, mean_visible=None):
+    """The `config` of both arms' lines."""
+    c = {"workload": WORKLOAD, "splats": args.splats, "width": args.width, "height": args.height, "sh_order": 3,
+         "depth_sorting": "Gpu", "blend": "unorm8", "poses": args.poses,
+         "l2": "inputs (1.4 GB scene) larger than L2", "parallelism": f"replicas x{world}"}
+    if mean_visible is not None:
+        c["mean_visible"] = int(mean_visible)
+    return c
+
+
 # ---------------------------------------------------------------------------------------------------
 class ClockSampler:
     """SM clock, power and clock-event reasons sampled DURING the timed region: NVML read through
@@ -289,14 +315,11 @@ def run_ours(args):
     t_end.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms_total = t_start.elapsed_time(t_end)
+    ms_total = reduce_max(t_start.elapsed_time(t_end))
     if world > 1:
-        tt = torch.tensor([ms_total], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(tt.item())
         torch.distributed.barrier()
     ms_per_step = ms_total / args.steps
-    value = world * args.steps / (ms_total / 1000.0)
+    value = job_throughput(args.steps, world, ms_total)
 
     # ---- per-stage timing (CUDA events on the launching streams), same frames ----
     r.set_profiling(True)
@@ -342,12 +365,8 @@ def run_ours(args):
         host.copy_(out, non_blocking=True)
         stream.synchronize()
     t1 = time.perf_counter()
-    e2e_ms = (t1 - t0) * 1000.0
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    e2e = {"value": round(world * e2e_frames / (e2e_ms / 1000.0), 2), "unit": "frames/s",
+    e2e_ms = reduce_max((t1 - t0) * 1000.0)
+    e2e = {"value": round(job_throughput(e2e_frames, world, e2e_ms), 2), "unit": "frames/s",
            "h2d_bytes_per_step": 64, "d2h_bytes_per_step": W * H * 4,
            "note": "spl_render_frame via ctypes (camera matrix from host memory) + RGBA8 image to pinned host, "
                    "synchronised every frame"}
@@ -392,10 +411,7 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered splats)",
-            "config": {"workload": WORKLOAD, "splats": args.splats, "width": W, "height": H,
-                       "sh_order": 3, "depth_sorting": "Gpu", "blend": "unorm8", "poses": args.poses,
-                       "mean_visible": int(vis_tot / frames_prof), "l2": "inputs (1.4 GB scene) larger than L2",
-                       "parallelism": f"replicas x{world}"},
+            "config": bench_config(args, world, vis_tot / frames_prof),
             "splats_per_s": round(value * args.splats, 0),
             "stages": stages, "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "cpu_baseline": cpu, "uhd": uhd, "differentiation": diff, "serving": serving,
@@ -710,7 +726,7 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": round(1000.0 * tot / args.steps, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered splats)",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "splats": args.splats, "width": args.width, "height": args.height},
+            "config": bench_config(args, world),
             "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -153,6 +153,23 @@ def test_frame_parity_modes(cuda, mode):
     assert_frame_parity(g, o, config)
 
 
+@pytest.mark.parametrize("w,h", [(1, 1), (17, 9), (1000, 3), (3, 700), (257, 255), (4112, 4112)])
+def test_viewports(cuda, w, h):
+    """Viewports that are not multiples of the 16-pixel tile, degenerate strips, one pixel, and one
+    with more than 65536 tiles (a 3-pass tile-id sort; up to 256 tiles take 1 pass)."""
+    n = 20000
+    config = Configuration(spherical_harmonics_order=3, max_splat_count=n, field_of_view_y=math.radians(60),
+                           max_pair_count=1 << 23)
+    rec = synthetic.plain_small(n, seed=31, sh_order=3)
+    rec[:, 55:58] += 1.0
+    cam = default_cam(dist=7.0)
+    g = gpu_frame(cuda, config, rec, cam, w, h)
+    o = oracle_frame(config, oracle.load_transform(rec), cam, w, h)
+    assert_frame_parity(g, o, config)
+    if w * h > 1000:
+        assert g[3].pair_count > 0
+
+
 @pytest.mark.parametrize("n", [0, 1, 2, 31, 1023, 1024, 1025, 4095, 4096, 4097, 8191, 12289])
 def test_tile_boundaries(cuda, n):
     config = Configuration(spherical_harmonics_order=1, max_splat_count=max(n, 1), field_of_view_y=math.radians(60))

@@ -93,11 +93,12 @@ __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict
     const uint32_t tile = s_tile, epoch = s_epoch, n = s.n;
     const uint32_t ntiles = (n + CULL_TILE - 1) / CULL_TILE;
     if (tile >= ntiles) return;  // a grid sized for a larger scene (captured frames)
-    const uint32_t base = tile * CULL_TILE + w * 512u + lane;
+    const uint32_t base = tile * CULL_TILE + w * (CULL_TILE / 8u) + lane;
 
-    float px[16], py[16], pz[16];
+    constexpr int PER_LANE = CULL_TILE / 256;
+    float px[PER_LANE], py[PER_LANE], pz[PER_LANE];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < PER_LANE; ++j) {
         const uint32_t e = base + 32u * j;
         if (e < n) {
             px[j] = __ldg(s.x + e);
@@ -107,11 +108,11 @@ __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict
             px[j] = py[j] = pz[j] = 0.0f;
         }
     }
-    uint32_t key[16], pos[16];
+    uint32_t key[PER_LANE], pos[PER_LANE];
     uint32_t vis_bits = 0u, wtotal = 0u, all_ones = 0u;
     const uint32_t lt = lanemask_lt();
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < PER_LANE; ++j) {
         const uint32_t e = base + 32u * j;
         float h[4];
 #pragma unroll
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict
     __syncthreads();
     const uint32_t out0 = s_base + wpre;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < PER_LANE; ++j) {
         if (vis_bits & (1u << j)) {
             keys_out[out0 + pos[j]] = key[j];
             idx_out[out0 + pos[j]] = base + 32u * j;

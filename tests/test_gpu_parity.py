@@ -283,6 +283,23 @@ def test_pair_capacity_overflow_is_an_error_not_a_fault(cuda):
     assert info.pair_count > 500
 
 
+@pytest.mark.parametrize("sorting", [DepthSorting.CPU, DepthSorting.GPU], ids=["cpu-fallback-keys", "gpu-keys"])
+def test_small_scene_640x480_parity(cuda, sorting):
+    """Config 'plain path, small scene' (the reference's CPU-runnable case): 100k splats, positions ~
+    N(0, 2^2), SH degree 0, 640x480, fovy 60, camera at distance 8 looking at the origin; with the CPU
+    depth-sort fallback's keys (what the reference runs on the CPU) and with the GPU keys."""
+    n = 100_000
+    config = Configuration(depth_sorting=sorting, spherical_harmonics_order=0, max_splat_count=n,
+                           field_of_view_y=math.radians(60))
+    rec = synthetic.plain_small(n, seed=0, sh_order=0)
+    cam = camera.look_at([0.0, 0.0, -8.0], [0.0, 0.0, 0.0])
+    g = gpu_frame(cuda, config, rec, cam, 640, 480)
+    o = oracle_frame(config, oracle.load_transform(rec), cam, 640, 480)
+    assert g[3].visible_count > 50000
+    assert_frame_parity(g, o, config)
+    assert image_psnr(g[0], o[0]) == float("inf")
+
+
 def test_clustered_1m_1080p_parity(cuda):
     """Config 'plain path 1M': 1M clustered splats, SH 3, 1920x1080, orbit poses (two of the 32)."""
     n = 1_000_000

@@ -232,10 +232,10 @@ def load_peaks():
 
 
 # DRAM traffic per unit of the dominant kernel, from one ncu capture of a smaller case of the same
-# workload (profiles/k_raster_3m_1080p.md: 3M splats, 1920x1080, 3,353,969 pairs, 237.8 MB read + 5.1
+# workload (profiles/k_raster_3m_1080p.md: 3M splats, 1920x1080, 3,353,969 pairs, 242.7 MB read + 7.2
 # MB written): the reads grow with the pairs, the image write is per launch.  The bench scales it to
 # its own frames by their pair counts.
-TRAFFIC_PER_UNIT = {"raster": {"per_pair": 237.8e6 / 3353969.0, "per_launch": 5.1e6,
+TRAFFIC_PER_UNIT = {"raster": {"per_pair": 242.7e6 / 3353969.0, "per_launch": 7.2e6,
                                "source": "profiles/k_raster_3m_1080p.md (3M-splat capture, scaled by pairs)"}}
 
 

@@ -10,8 +10,9 @@
 //   k_tile_ranges  - start/end of each tile's run in the sorted pair list
 //   k_tile_order   - the raster's tile order: most pairs first
 //   k_raster       - one CTA per tile, one thread per pixel; records staged through shared memory in
-//                    batches of 256, warp-uniform box rejection, exact coverage test, falloff, blend,
-//                    and early exit once every pixel of the tile is opaque
+//                    batches of 256, per-pixel record lists from the boxes (bit-transposed ballots),
+//                    exact coverage test, falloff, blend, and early exit once every pixel of the tile
+//                    is opaque
 #include "spl_device.cuh"
 
 namespace spl {
@@ -225,17 +226,18 @@ __global__ void __launch_bounds__(1024) k_tile_order(const uint2* __restrict__ r
 // ------------------------------------------------------------------------------------------------
 constexpr int RASTER_BATCH = 256;
 
-// One CTA per 16x16 tile, one thread per pixel.  Warp w owns rows 2w, 2w+1, split into eight 2x2-pixel
-// groups of 4 lanes (group g = lane / 4 covers columns 2g, 2g+1).  The tile's records (depth order)
-// are staged through shared memory in batches of 256.  For each chunk of 32 records a lane tests one
-// record's pixel box against the eight groups' blocks; eight ballots give each group its relevance
-// list, in order.  The warp then walks the eight lists at once: in every iteration each group takes
-// its next record, so one pass of the per-pixel code serves up to eight splats (most splats here
-// cover a few pixels, so small groups keep far more lanes busy than a whole warp per splat).  Per
-// pixel: box test, coverage test, falloff, 1/255 discard, blend — the operations of the oracle's
-// raster_tile in the same order, so the image is bit-identical.  Lists are walked in depth order per
-// pixel, a warp whose pixels are all finished skips the rest, and the CTA stops once every pixel is
-// finished (T == 0 in unorm8 mode, T < 1e-4 in fp32 mode).
+// One CTA per 16x16 tile, one thread per pixel.  Warp w owns the strip of rows 2w, 2w+1; lane l holds
+// column 2 (l / 4) + (l & 1) and row 2w + ((l >> 1) & 1), so the strip's 2x2 blocks are groups of four
+// lanes.  The tile's records (depth order) are staged through shared memory in batches of 256.  For
+// each step of 32 records a lane tests one record against the strip and forms the mask of the lanes
+// (pixels) it may draw; a warp-wide bit transpose turns the 32 masks into each pixel's list of the 32
+// records.  The warp then walks the 32 lists of the whole batch at once: in every iteration each pixel
+// takes its next record, so one pass of the per-pixel code serves as many splats as there are lanes
+// with work (most splats here cover a few pixels).  Per pixel: coverage test, falloff, 1/255
+// discard, blend — the operations of the oracle's raster_tile in the same order, so the image is
+// bit-identical.  Lists are walked in depth order per pixel, a warp whose pixels are all finished
+// skips the rest, and the CTA stops once every pixel is finished (T == 0 in unorm8 mode, T < 1e-4 in
+// fp32 mode).
 // Block indices g (of the eight along a warp's strip) with |c + s g| <= T, widened conservatively:
 // the quotients are clamped to [-1, 9] before rounding outwards, so their float error (a few ulp of
 // at most 9) stays far below the 1e-3 widening.  Empty when lo > hi.
@@ -253,14 +255,36 @@ __device__ __forceinline__ void g_interval(float c, float s, float T, int& lo, i
     hi = (int)floorf(b + 1e-3f);
 }
 
+// Lanes of a warp's 2x16-pixel strip whose column is >= c (0 <= c <= 16); lane l holds column
+// 2 (l / 4) + (l & 1) and row (l >> 1) & 1.
+__device__ __forceinline__ uint32_t strip_columns_from(int c) {
+    const int k = c >> 1;
+    if (c & 1) return (uint32_t)(0xFFFFFFFFull << (4 * k + 4)) | (uint32_t)(0xAull << (4 * k));
+    return (uint32_t)(0xFFFFFFFFull << (4 * k));
+}
+
+// 32x32 bit-matrix transpose across the warp: bit i of the result in lane l is bit l of x in lane i.
+// Each step d exchanges lane-index bit d with bit-index bit d.
+__device__ __forceinline__ uint32_t transpose_lane_bits(uint32_t x, uint32_t lane) {
+    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const uint32_t d = 16u >> k, m = masks[k];
+        const uint32_t p = __shfl_xor_sync(FULL_MASK, x, (int)d);
+        x = (lane & d) ? ((x & ~m) | ((p >> d) & m)) : ((x & m) | ((p & m) << d));
+    }
+    return x;
+}
+
 template <bool RECT, int BLEND>
-__global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ tile_order,
+__global__ void __launch_bounds__(256, 5) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ tile_order,
                                                 const uint32_t* __restrict__ pair_vals,
                                                 const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
                                                 float psx, float psy, void* __restrict__ out) {
     __shared__ float4 s_q0[RASTER_BATCH], s_q1[RASTER_BATCH], s_q2[RASTER_BATCH];
     __shared__ float4 s_q3[RECT ? 1 : RASTER_BATCH];
     __shared__ float s_lut[256];
+    __shared__ uint32_t s_plist[RASTER_BATCH / 32][256];  // [word][pixel]: the pixels' record lists of the batch
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     const uint32_t grp = lane >> 2, li = lane & 3u;
     const int tile = tile_order ? (int)__ldg(tile_order + blockIdx.x) : (int)blockIdx.x;
@@ -292,97 +316,100 @@ __global__ void __launch_bounds__(256) k_raster(const uint2* __restrict__ ranges
         __syncthreads();
         const uint32_t cnt = min((uint32_t)RASTER_BATCH, rg.y - b);
         if (!warp_done) {
-            for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
-                // pixels finished: the warp leaves, a finished 2x2 group walks no list
-                const uint32_t dmask = __ballot_sync(FULL_MASK, done);
-                if (dmask == FULL_MASK) break;
-                const bool grp_done = ((dmask >> (4u * grp)) & 0xFu) == 0xFu;
-                // relevance of record j0 + lane for each of the warp's eight blocks as an interval
-                // [ga, gb] of block indices; `mine` keeps the ballot of this lane's block.  A block is
-                // relevant when the record's pixel box meets it and, for rectangles, when some pixel
-                // centre of it may lie in the rectangle: over the block's four centres tc lies within
-                // tc(block centre) +- ext (half the block's extent mapped by |A|, widened by a rounding
-                // bound far above the per-pixel FMA chains' error), and along the warp's strip the
-                // block centre's tc is c + 2g A, so |c + 2g A| <= margin + ext is an interval of g.
-                // Skipped blocks hold no drawn pixel: the image is unchanged.
-                int ga = 1, gb = 0;
-                {
-                    const uint32_t jl = j0 + lane;
-                    if (jl < cnt) {
-                        const float4 r1 = s_q1[jl];
-                        const uint32_t lo = __float_as_uint(r1.w), hi = __float_as_uint(s_q2[jl].w);
-                        const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
-                        const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
-                        if (!(y1 < by0 || y0 > by0 + 1) && x0 <= x1) {
-                            // block g covers columns wx0 + 2g, wx0 + 2g + 1 (floor halves: arithmetic shifts)
-                            ga = (x0 - wx0) >> 1;
-                            gb = (x1 - wx0) >> 1;
-                            if (RECT) {
-                                const float4 r0 = s_q0[jl];
-                                const float Xc = (float)(wx0 + 1), Yc = (float)(by0 + 1);  // block 0's centre
-                                const float Xm = (float)(wx0 + 16), Ym = (float)(by0 + 2);
-                                const float cx = fmaf(r0.y, Yc, fmaf(r0.x, Xc, r0.z));
-                                const float cy = fmaf(r1.x, Yc, fmaf(r0.w, Xc, r1.y));
-                                const float Tx = margin + 0.5f * (fabsf(r0.x) + fabsf(r0.y)) +
-                                                 1e-6f * (fabsf(r0.x) * Xm + fabsf(r0.y) * Ym + fabsf(r0.z));
-                                const float Ty = margin + 0.5f * (fabsf(r0.w) + fabsf(r1.x)) +
-                                                 1e-6f * (fabsf(r0.w) * Xm + fabsf(r1.x) * Ym + fabsf(r1.y));
-                                int lx, hx, ly, hy;
-                                g_interval(cx, 2.0f * r0.x, Tx, lx, hx);
-                                g_interval(cy, 2.0f * r0.w, Ty, ly, hy);
-                                ga = max(ga, max(lx, ly));
-                                gb = min(gb, min(hx, hy));
-                            }
+            // Per-pixel lists of the batch, 32 records per step.  Lane l tests record 32c + l against
+            // the warp's 2x16-pixel strip: the pixels inside the record's pixel box, and, for
+            // rectangles, only in the 2x2 blocks where some pixel centre may lie in the rectangle:
+            // over a block's four centres tc lies within tc(block centre) +- ext (half the block's
+            // extent mapped by |A|, widened by a rounding bound far above the per-pixel FMA chains'
+            // error), and along the strip the block centre's tc is c + 2g A, so |c + 2g A| <= margin +
+            // ext is an interval of block indices g.  Skipped pixels are not drawn by the record: the
+            // image is unchanged.  The 32 lane masks are transposed so that lane p holds word c of
+            // pixel p's list (bit i: record 32c + i), kept in s_plist; bit c of `nz` marks a non-empty
+            // word.
+            uint32_t nz = 0u;
+            for (uint32_t c = 0; c * 32u < cnt; ++c) {
+                uint32_t pm = 0u;
+                const uint32_t jl = c * 32u + lane;
+                if (jl < cnt) {
+                    const float4 r1 = s_q1[jl];
+                    const uint32_t lo = __float_as_uint(r1.w), hi = __float_as_uint(s_q2[jl].w);
+                    const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
+                    const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
+                    if (!(y1 < by0 || y0 > by0 + 1) && x0 <= x1) {
+                        int ca = x0 - wx0, cb = x1 - wx0;  // strip columns of the box
+                        if (RECT) {
+                            const float4 r0 = s_q0[jl];
+                            const float Xc = (float)(wx0 + 1), Yc = (float)(by0 + 1);  // block 0's centre
+                            const float Xm = (float)(wx0 + 16), Ym = (float)(by0 + 2);
+                            const float cx = fmaf(r0.y, Yc, fmaf(r0.x, Xc, r0.z));
+                            const float cy = fmaf(r1.x, Yc, fmaf(r0.w, Xc, r1.y));
+                            const float Tx = margin + 0.5f * (fabsf(r0.x) + fabsf(r0.y)) +
+                                             1e-6f * (fabsf(r0.x) * Xm + fabsf(r0.y) * Ym + fabsf(r0.z));
+                            const float Ty = margin + 0.5f * (fabsf(r0.w) + fabsf(r1.x)) +
+                                             1e-6f * (fabsf(r0.w) * Xm + fabsf(r1.x) * Ym + fabsf(r1.y));
+                            int lx, hx, ly, hy;
+                            g_interval(cx, 2.0f * r0.x, Tx, lx, hx);
+                            g_interval(cy, 2.0f * r0.w, Ty, ly, hy);
+                            ca = max(ca, 2 * max(lx, ly));
+                            cb = min(cb, 2 * min(hx, hy) + 1);
+                        }
+                        ca = max(ca, 0);
+                        cb = min(cb, 15);
+                        if (ca <= cb) {
+                            pm = strip_columns_from(ca) & ~strip_columns_from(cb + 1);
+                            if (y0 > by0) pm &= 0xCCCCCCCCu;      // lanes of the strip's second row
+                            if (y1 < by0 + 1) pm &= 0x33333333u;  // lanes of its first row
                         }
                     }
                 }
-                uint32_t mine = 0u;
-#pragma unroll
-                for (int g = 0; g < 8; ++g) {
-                    const uint32_t m = __ballot_sync(FULL_MASK, ga <= g && g <= gb);
-                    mine = (int)grp == g ? m : mine;
+                const uint32_t t = transpose_lane_bits(pm, lane);
+                s_plist[c][tid] = t;
+                nz |= (t != 0u ? 1u : 0u) << c;
+            }
+            // Walk the 32 lists at once across the whole batch: in every iteration each pixel takes its
+            // next record.  The warp leaves once every pixel is finished or has walked its list.
+            uint32_t cur = 0u, cbase = 0u;
+            while (true) {
+                if (cur == 0u && nz != 0u) {
+                    const uint32_t c = (uint32_t)(__ffs(nz) - 1);
+                    nz &= nz - 1u;
+                    cur = s_plist[c][tid];
+                    cbase = c * 32u;
                 }
-                if (grp_done) mine = 0u;
-                while (__any_sync(FULL_MASK, mine != 0u)) {
-                    if (mine == 0u) continue;
-                    const uint32_t j = j0 + (uint32_t)(__ffs(mine) - 1);
-                    mine &= mine - 1u;
-                    const float4 q1 = s_q1[j], q2 = s_q2[j];
-                    const uint32_t lo = __float_as_uint(q1.w), hi = __float_as_uint(q2.w);
-                    const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
-                    const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
-                    if (done || (unsigned)(px - x0) > (unsigned)(x1 - x0) || (unsigned)(py - y0) > (unsigned)(y1 - y0))
-                        continue;
-                    const float4 q0 = s_q0[j];
-                    const float tcx = fmaf(q0.y, Y, fmaf(q0.x, X, q0.z));
-                    const float tcy = fmaf(q1.x, Y, fmaf(q0.w, X, q1.y));
-                    if (RECT) {
-                        if (!(fabsf(tcx) <= margin && fabsf(tcy) <= margin)) continue;
-                    } else {
-                        const float4 q3 = s_q3[j];
-                        const float dx = fmaf(psx, X, q3.x), dy = fmaf(psy, Y, q3.y);
-                        if (!(fabsf(dx) <= q3.z && fabsf(dy) <= q3.z)) continue;
-                    }
-                    const float power = fmaf(tcx, tcx, tcy * tcy);
-                    const float alpha = q1.z * spl_expf_nonpos(-0.5f * power);
-                    if (alpha < alpha_min) continue;
-                    // __saturatef == clamp to [0, 1] (NaN -> 0); __float2int_rn == (int)rintf
-                    const float sr = __saturatef(q2.x * alpha), sg = __saturatef(q2.y * alpha);
-                    const float sb = __saturatef(q2.z * alpha), sa = __saturatef(alpha);
-                    if (BLEND == 0) {
-                        const float dA = s_lut[ta];
-                        cr = __float2int_rn(__saturatef(sr * dA + s_lut[cr]) * 255.0f);
-                        cg = __float2int_rn(__saturatef(sg * dA + s_lut[cg]) * 255.0f);
-                        cb = __float2int_rn(__saturatef(sb * dA + s_lut[cb]) * 255.0f);
-                        ta = __float2int_rn(__saturatef(dA * (1.0f - sa)) * 255.0f);
-                        done = ta == 0;
-                    } else {
-                        fr = sr * ft + fr;
-                        fg = sg * ft + fg;
-                        fb = sb * ft + fb;
-                        ft = ft * (1.0f - sa);
-                        done = ft < FP32_T_MIN;
-                    }
+                if (!__any_sync(FULL_MASK, cur != 0u && !done)) break;
+                if (cur == 0u || done) continue;
+                const uint32_t j = cbase + (uint32_t)(__ffs(cur) - 1);
+                cur &= cur - 1u;
+                const float4 q1 = s_q1[j], q2 = s_q2[j];
+                const float4 q0 = s_q0[j];
+                const float tcx = fmaf(q0.y, Y, fmaf(q0.x, X, q0.z));
+                const float tcy = fmaf(q1.x, Y, fmaf(q0.w, X, q1.y));
+                if (RECT) {
+                    if (!(fabsf(tcx) <= margin && fabsf(tcy) <= margin)) continue;
+                } else {
+                    const float4 q3 = s_q3[j];
+                    const float dx = fmaf(psx, X, q3.x), dy = fmaf(psy, Y, q3.y);
+                    if (!(fabsf(dx) <= q3.z && fabsf(dy) <= q3.z)) continue;
+                }
+                const float power = fmaf(tcx, tcx, tcy * tcy);
+                const float alpha = q1.z * spl_expf_nonpos(-0.5f * power);
+                if (alpha < alpha_min) continue;
+                // __saturatef == clamp to [0, 1] (NaN -> 0); __float2int_rn == (int)rintf
+                const float sr = __saturatef(q2.x * alpha), sg = __saturatef(q2.y * alpha);
+                const float sb = __saturatef(q2.z * alpha), sa = __saturatef(alpha);
+                if (BLEND == 0) {
+                    const float dA = s_lut[ta];
+                    cr = __float2int_rn(__saturatef(sr * dA + s_lut[cr]) * 255.0f);
+                    cg = __float2int_rn(__saturatef(sg * dA + s_lut[cg]) * 255.0f);
+                    cb = __float2int_rn(__saturatef(sb * dA + s_lut[cb]) * 255.0f);
+                    ta = __float2int_rn(__saturatef(dA * (1.0f - sa)) * 255.0f);
+                    done = ta == 0;
+                } else {
+                    fr = sr * ft + fr;
+                    fg = sg * ft + fg;
+                    fb = sb * ft + fb;
+                    ft = ft * (1.0f - sa);
+                    done = ft < FP32_T_MIN;
                 }
             }
             warp_done = __all_sync(FULL_MASK, done);

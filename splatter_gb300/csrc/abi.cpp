@@ -304,7 +304,7 @@ static int render_frame_impl(spl_renderer* r, const SceneView& sv, const Uniform
     const bool coop = r->sort_mode == SPL_SORT_COOPERATIVE;
     r->mark(0, st);
     launch_frame_begin(r->fc, r->epoch, u, r->d_u, sv, r->d_sv, st);
-    launch_cull_key(mode, N, r->d_sv, r->d_u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
+    launch_cull_key(mode, !coop, N, r->d_sv, r->d_u, r->fc, r->epoch, r->st_cull, r->keys_a, r->idx, sl, st);
     r->mark(1, st);
     launch_preprocess((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
                       cfg.use_unaligned_rectangles != 0, r->d_sv, r->d_u, r->idx, r->fc, r->rec, r->boxes, N, st);
@@ -336,7 +336,7 @@ static int render_frame_impl(spl_renderer* r, const SceneView& sv, const Uniform
     }
     r->mark(3, st);
     CU(cudaMemsetAsync(r->ranges, 0, tiles * sizeof(uint2), st));
-    launch_bin(mode, order, r->boxes, r->fc, r->epoch, r->st_bin, r->pk_a, r->pv_a, (uint32_t)r->pair_cap,
+    launch_bin(mode, !coop, order, r->boxes, r->fc, r->epoch, r->st_bin, r->pk_a, r->pv_a, (uint32_t)r->pair_cap,
                (int)tiles_x, N, sl, st);
     r->mark(4, st);
     // stable sort of the pairs by tile id keeps each tile's list in depth order

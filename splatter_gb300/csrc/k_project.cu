@@ -69,19 +69,20 @@ __device__ __forceinline__ void stage_frame(const Uniforms* __restrict__ d_u, Un
 // Cull + key + histogram + ordered compaction.  One CTA handles 4096 consecutive splats; warp w owns
 // splats [w*512, w*512+512) of the tile and lane l handles elements w*512 + 32*j + l, so loads are
 // coalesced and the ballot order is the index order.
-template <int MODE>
+template <int MODE, bool HIST>
 __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict__ d_sv, const Uniforms* __restrict__ d_u,
                                                   FrameCounters* fc,
                                                   const uint32_t* __restrict__ epoch_word, uint64_t* status,
                                                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ idx_out,
                                                   uint32_t spin_limit) {
-    __shared__ uint32_t s_hist[1024];
+    __shared__ uint32_t s_hist[HIST ? 1024 : 1];
     __shared__ uint32_t s_wcnt[8];
     __shared__ uint32_t s_tile, s_epoch, s_base;
     __shared__ Uniforms s_u;
     __shared__ SceneView s_sv;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
-    for (uint32_t i = tid; i < 1024u; i += 256u) s_hist[i] = 0u;
+    if (HIST)
+        for (uint32_t i = tid; i < 1024u; i += 256u) s_hist[i] = 0u;
     stage_frame(d_u, s_u, d_sv, s_sv);
     if (tid == 0) {
         s_tile = atomicAdd(&fc->tile_counter[0], 1u);
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict
         }
     }
     uint32_t key[PER_LANE], pos[PER_LANE];
-    uint32_t vis_bits = 0u, wtotal = 0u, all_ones = 0u;
+    uint32_t vis_bits = 0u, wtotal = 0u, all_ones = 0u, top_ff = 0u;
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int j = 0; j < PER_LANE; ++j) {
@@ -142,11 +143,14 @@ __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict
         key[j] = k;
         if (vis) {
             vis_bits |= 1u << j;
-            atomicAdd(&s_hist[k & 255u], 1u);
-            atomicAdd(&s_hist[256u + ((k >> 8) & 255u)], 1u);
-            atomicAdd(&s_hist[512u + ((k >> 16) & 255u)], 1u);
-            atomicAdd(&s_hist[768u + (k >> 24)], 1u);
+            if (HIST) {
+                atomicAdd(&s_hist[k & 255u], 1u);
+                atomicAdd(&s_hist[256u + ((k >> 8) & 255u)], 1u);
+                atomicAdd(&s_hist[512u + ((k >> 16) & 255u)], 1u);
+                atomicAdd(&s_hist[768u + (k >> 24)], 1u);
+            }
             all_ones += k == 0xFFFFFFFFu;
+            top_ff += (k >> 24) == 0xFFu;
         }
     }
     if (lane == 0) s_wcnt[w] = wtotal;
@@ -176,25 +180,27 @@ __global__ void __launch_bounds__(256, 3) k_cull_key(const SceneView* __restrict
             idx_out[out0 + pos[j]] = base + 32u * j;
         }
     }
-    for (uint32_t i = tid; i < 1024u; i += 256u) {
-        const uint32_t v = s_hist[i];
-        if (v) atomicAdd(&fc->hist_depth[0][0] + i, v);
+    if (HIST) {
+        for (uint32_t i = tid; i < 1024u; i += 256u) {
+            const uint32_t v = s_hist[i];
+            if (v) atomicAdd(&fc->hist_depth[0][0] + i, v);
+        }
     }
     if (MODE != DS_CPU) {
-        const uint32_t a = __reduce_add_sync(FULL_MASK, all_ones);
+        const uint32_t a = __reduce_add_sync(FULL_MASK, all_ones), t = __reduce_add_sync(FULL_MASK, top_ff);
         if (lane == 0 && a) atomicAdd(&fc->keys_all_ones, a);
+        if (lane == 0 && t) atomicAdd(&fc->keys_top_ff, t);
     }
 }
 
-void launch_cull_key(int mode, uint32_t grid_n, const SceneView* d_sv, const Uniforms* u, FrameCounters* fc,
-                     const uint32_t* epoch_word, uint64_t* status, uint32_t* keys_out, uint32_t* idx_out,
-                     uint32_t spin_limit, cudaStream_t st) {
+void launch_cull_key(int mode, bool hist, uint32_t grid_n, const SceneView* d_sv, const Uniforms* u,
+                     FrameCounters* fc, const uint32_t* epoch_word, uint64_t* status, uint32_t* keys_out,
+                     uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st) {
     if (grid_n == 0) return;
     const uint32_t grid = (grid_n + CULL_TILE - 1) / CULL_TILE;
-    if (mode == DS_CPU)
-        k_cull_key<DS_CPU><<<grid, 256, 0, st>>>(d_sv, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
-    else
-        k_cull_key<DS_GPU><<<grid, 256, 0, st>>>(d_sv, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
+    auto k = mode == DS_CPU ? (hist ? k_cull_key<DS_CPU, true> : k_cull_key<DS_CPU, false>)
+                            : (hist ? k_cull_key<DS_GPU, true> : k_cull_key<DS_GPU, false>);
+    k<<<grid, 256, 0, st>>>(d_sv, u, fc, epoch_word, status, keys_out, idx_out, spin_limit);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -18,7 +18,7 @@
 namespace spl {
 
 // ------------------------------------------------------------------------------------------------
-template <bool ORDERED>
+template <bool ORDERED, bool HIST>
 __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order, const uint2* __restrict__ boxes,
                                              FrameCounters* fc, int mode, const uint32_t* __restrict__ epoch_word,
                                              uint64_t* status, uint32_t* __restrict__ pair_keys,
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
     __shared__ uint32_t s_slot[BIN_TILE];
     __shared__ uint32_t s_box[BIN_TILE];  // tx0 | ty0 << 16
     __shared__ uint16_t s_bw[BIN_TILE];
-    __shared__ uint32_t s_hist[768];
+    __shared__ uint32_t s_hist[HIST ? 768 : 1];
     __shared__ uint32_t s_scan[8];
     __shared__ uint32_t s_tile, s_epoch, s_base, s_draw;
     const uint32_t tid = threadIdx.x;
@@ -38,12 +38,14 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
         const uint32_t V = fc->visible;
         uint32_t draw = V;
         if (mode == DS_GPU) draw = V - fc->keys_all_ones;
-        else if (mode == DS_GPU_INDIRECT) draw = V - fc->hist_depth[3][255];
+        else if (mode == DS_GPU_INDIRECT) draw = V - fc->keys_top_ff;
         s_draw = draw;
     }
-    s_hist[tid] = 0u;
-    s_hist[tid + 256] = 0u;
-    s_hist[tid + 512] = 0u;
+    if (HIST) {
+        s_hist[tid] = 0u;
+        s_hist[tid + 256] = 0u;
+        s_hist[tid + 512] = 0u;
+    }
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch, draw = s_draw;
     const uint32_t ntiles = (draw + BIN_TILE - 1) / BIN_TILE;
@@ -117,28 +119,29 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
         if (g < pair_cap) {
             pair_keys[g] = tid_tile;
             pair_vals[g] = s_slot[lo];
-            atomicAdd(&s_hist[tid_tile & 255u], 1u);
-            atomicAdd(&s_hist[256u + ((tid_tile >> 8) & 255u)], 1u);
-            atomicAdd(&s_hist[512u + ((tid_tile >> 16) & 255u)], 1u);
+            if (HIST) {
+                atomicAdd(&s_hist[tid_tile & 255u], 1u);
+                atomicAdd(&s_hist[256u + ((tid_tile >> 8) & 255u)], 1u);
+                atomicAdd(&s_hist[512u + ((tid_tile >> 16) & 255u)], 1u);
+            }
         }
     }
-    __syncthreads();
-    for (uint32_t i = tid; i < 768u; i += 256u) {
-        const uint32_t v = s_hist[i];
-        if (v) atomicAdd(&fc->hist_pairs[0][0] + i, v);
+    if (HIST) {
+        __syncthreads();
+        for (uint32_t i = tid; i < 768u; i += 256u) {
+            const uint32_t v = s_hist[i];
+            if (v) atomicAdd(&fc->hist_pairs[0][0] + i, v);
+        }
     }
 }
 
-void launch_bin(int mode, const uint32_t* order, const uint2* boxes, FrameCounters* fc, const uint32_t* epoch_word,
-                uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals, uint32_t pair_cap, int tiles_x,
-                uint32_t max_n, uint32_t spin_limit, cudaStream_t st) {
+void launch_bin(int mode, bool hist, const uint32_t* order, const uint2* boxes, FrameCounters* fc,
+                const uint32_t* epoch_word, uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals,
+                uint32_t pair_cap, int tiles_x, uint32_t max_n, uint32_t spin_limit, cudaStream_t st) {
     const uint32_t grid = max_n == 0 ? 1u : (max_n + BIN_TILE - 1) / BIN_TILE;
-    if (order)
-        k_bin<true><<<grid, 256, 0, st>>>(order, boxes, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
-                                          tiles_x, spin_limit);
-    else
-        k_bin<false><<<grid, 256, 0, st>>>(order, boxes, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap,
-                                           tiles_x, spin_limit);
+    auto k = order ? (hist ? k_bin<true, true> : k_bin<true, false>) : (hist ? k_bin<false, true> : k_bin<false, false>);
+    k<<<grid, 256, 0, st>>>(order, boxes, fc, mode, epoch_word, status, pair_keys, pair_vals, pair_cap, tiles_x,
+                            spin_limit);
 }
 
 // ------------------------------------------------------------------------------------------------

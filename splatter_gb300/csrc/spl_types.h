@@ -33,13 +33,14 @@ struct FrameCounters {
     uint32_t tile_counter[12];  // dynamic tile ids: 0 cull, 1..4 depth passes, 5..7 pair passes, 8 bin
     uint32_t visible;          // V: splats that pass the frustum test
     uint32_t keys_all_ones;    // visible splats whose composite key is 0xFFFFFFFF
+    uint32_t keys_top_ff;      // visible splats whose key's top byte is 0xFF (not drawn in indirect mode)
     uint32_t pairs;            // (tile, splat) pairs the binning wanted to emit
     uint32_t err;              // SPL_DEV_ERR_* bits
     uint32_t draw;             // entries drawn (mode dependent)
     uint32_t epoch;            // copy of the frame epoch (for readback)
     uint32_t barrier[2];       // grid barrier of the cooperative sort: arrivals, generation
-    uint32_t hist_depth[4][256];  // digit histograms of the visible depth keys
-    uint32_t hist_pairs[3][256];  // digit histograms of the tile ids of all pairs
+    uint32_t hist_depth[4][256];  // digit histograms of the visible depth keys (onesweep sort only)
+    uint32_t hist_pairs[3][256];  // digit histograms of the tile ids of all pairs (onesweep sort only)
 };
 
 // Depth-sorting modes (renderer.rs:14-23).
@@ -74,9 +75,10 @@ void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, const Uniforms&
 const void* frame_begin_kernel();  // host handle of k_frame_begin (to find its node in a captured graph)
 // grid_n: the splat count the grid is sized for (the scene's, or the renderer's maximum for a
 // captured frame whose scene changes between launches); the kernels read the scene from d_sv.
-void launch_cull_key(int mode, uint32_t grid_n, const SceneView* d_sv, const Uniforms* d_u, FrameCounters* fc,
-                     const uint32_t* epoch_word,
-                     uint64_t* status, uint32_t* keys_out, uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st);
+// hist: also build the digit histograms of the keys (the onesweep passes need them).
+void launch_cull_key(int mode, bool hist, uint32_t grid_n, const SceneView* d_sv, const Uniforms* d_u,
+                     FrameCounters* fc, const uint32_t* epoch_word, uint64_t* status, uint32_t* keys_out,
+                     uint32_t* idx_out, uint32_t spin_limit, cudaStream_t st);
 void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView* d_sv, const Uniforms* d_u,
                        const uint32_t* idx, const FrameCounters* fc, float4* rec, uint2* boxes, uint32_t max_n,
                        cudaStream_t st);
@@ -87,9 +89,10 @@ void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t*
                      const uint32_t* n_ptr, uint32_t n_cap, const uint32_t* hist256, uint64_t* status,
                      uint32_t* tile_counter, const uint32_t* epoch_word, int shift, uint32_t spin_limit,
                      uint32_t* err, cudaStream_t st);
-void launch_bin(int mode, const uint32_t* order, const uint2* boxes, FrameCounters* fc, const uint32_t* epoch_word,
-                uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals, uint32_t pair_cap, int tiles_x,
-                uint32_t max_n, uint32_t spin_limit, cudaStream_t st);
+// hist: also build the digit histograms of the pairs' tile ids (the onesweep passes need them).
+void launch_bin(int mode, bool hist, const uint32_t* order, const uint2* boxes, FrameCounters* fc,
+                const uint32_t* epoch_word, uint64_t* status, uint32_t* pair_keys, uint32_t* pair_vals,
+                uint32_t pair_cap, int tiles_x, uint32_t max_n, uint32_t spin_limit, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint32_t pair_cap, uint2* ranges,
                         cudaStream_t st);
 // Orders the tiles most pairs first (tile_order, one entry per tile), then rasterises them in that order;

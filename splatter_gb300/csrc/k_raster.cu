@@ -231,28 +231,27 @@ constexpr int RASTER_BATCH = 256;
 
 // One CTA per 16x16 tile, one thread per pixel.  Warp w owns the strip of rows 2w, 2w+1; lane l holds
 // column 2 (l / 4) + (l & 1) and row 2w + ((l >> 1) & 1), so the strip's 2x2 blocks are groups of four
-// lanes.  The tile's records (depth order) are staged through shared memory in batches of 256.  For
-// each step of 32 records a lane tests one record against the strip and forms the mask of the lanes
-// (pixels) it may draw; a warp-wide bit transpose turns the 32 masks into each pixel's list of the 32
-// records.  The warp then walks the 32 lists of the whole batch at once: in every iteration each pixel
-// takes its next record, so one pass of the per-pixel code serves as many splats as there are lanes
-// with work (most splats here cover a few pixels).  Per pixel: coverage test, falloff, 1/255
-// discard, blend — the operations of the oracle's raster_tile in the same order, so the image is
-// bit-identical.  Lists are walked in depth order per pixel, a warp whose pixels are all finished
-// skips the rest, and the CTA stops once every pixel is finished (T == 0 in unorm8 mode, T < 1e-4 in
-// fp32 mode).
+// lanes.  The tile's records (depth order) are staged through shared memory in batches of 256; the
+// thread staging a record also forms its mask of the lanes (pixels) it may draw in each of the eight
+// strips.  For each step of 32 records a warp-wide bit transpose turns its strip's 32 masks into each
+// pixel's list of the 32 records.  The warp then walks the 32 lists of the whole batch at once: in
+// every iteration each pixel takes its next record, so one pass of the per-pixel code serves as many
+// splats as there are lanes with work (most splats here cover a few pixels).  Per pixel: coverage
+// test, falloff, 1/255 discard, blend — the operations of the oracle's raster_tile in the same order,
+// so the image is bit-identical.  Lists are walked in depth order per pixel, a warp whose pixels are
+// all finished skips the rest, and the CTA stops once every pixel is finished (T == 0 in unorm8 mode,
+// T < 1e-4 in fp32 mode).
 // Block indices g (of the eight along a warp's strip) with |c + s g| <= T, widened conservatively:
 // the quotients are clamped to [-1, 9] before rounding outwards, so their float error (a few ulp of
 // at most 9) stays far below the 1e-3 widening.  Empty when lo > hi.
-__device__ __forceinline__ void g_interval(float c, float s, float T, int& lo, int& hi) {
+__device__ __forceinline__ void g_interval(float c, float s, float rs, float T, int& lo, int& hi) {
     if (fabsf(s) < 1e-30f) {
         const bool all = fabsf(c) <= T;
         lo = all ? -1 : 1;
         hi = all ? 9 : 0;
         return;
     }
-    const float rs = 1.0f / s;  // IEEE: finite and within half an ulp for every finite s here
-    const float q1 = (-T - c) * rs, q2 = (T - c) * rs;
+    const float q1 = (-T - c) * rs, q2 = (T - c) * rs;  // rs = 1 / s (IEEE: finite, within half an ulp)
     const float a = fminf(fmaxf(fminf(q1, q2), -1.0f), 9.0f), b = fminf(fmaxf(fmaxf(q1, q2), -1.0f), 9.0f);
     lo = (int)ceilf(a - 1e-3f);
     hi = (int)floorf(b + 1e-3f);
@@ -280,13 +279,14 @@ __device__ __forceinline__ uint32_t transpose_lane_bits(uint32_t x, uint32_t lan
 }
 
 template <bool RECT, int BLEND>
-__global__ void __launch_bounds__(256, 5) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ tile_order,
+__global__ void __launch_bounds__(256, 6) k_raster(const uint2* __restrict__ ranges, const uint32_t* __restrict__ tile_order,
                                                 const uint32_t* __restrict__ pair_vals,
                                                 const float4* __restrict__ rec, int W, int H, int tiles_x, float margin,
                                                 float psx, float psy, void* __restrict__ out) {
     __shared__ float4 s_q0[RASTER_BATCH], s_q1[RASTER_BATCH], s_q2[RASTER_BATCH];
     __shared__ float4 s_q3[RECT ? 1 : RASTER_BATCH];
     __shared__ float s_lut[256];
+    __shared__ uint32_t s_pm[8][RASTER_BATCH];             // [strip][record]: lane masks of the batch's records
     __shared__ uint32_t s_plist[RASTER_BATCH / 32][256];  // [word][pixel]: the pixels' record lists of the batch
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
     const uint32_t grp = lane >> 2, li = lane & 3u;
@@ -311,61 +311,72 @@ __global__ void __launch_bounds__(256, 5) k_raster(const uint2* __restrict__ ran
         if (i < rg.y) {
             const uint32_t slot = __ldg(pair_vals + i);
             const float4* r = rec + (size_t)slot * 4;
-            s_q0[tid] = __ldg(r + 0);
-            s_q1[tid] = __ldg(r + 1);
-            s_q2[tid] = __ldg(r + 2);
+            const float4 r0 = __ldg(r + 0), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
+            s_q0[tid] = r0;
+            s_q1[tid] = r1;
+            s_q2[tid] = r2;
             if (!RECT) s_q3[tid] = __ldg(r + 3);
+            // The record's lane mask for each of the tile's eight strips (rows 2w, 2w + 1): the pixels
+            // inside its pixel box and, for rectangles, only in the 2x2 blocks where some pixel
+            // centre may lie in the rectangle: over a block's four centres tc lies within tc(block
+            // centre) +- ext (half the block's extent mapped by |A|, widened by a rounding bound far
+            // above the per-pixel FMA chains' error), and along the strip the block centre's tc is
+            // c + 2g A, so |c + 2g A| <= margin + ext is an interval of block indices g.  Skipped
+            // pixels are not drawn by the record: the image is unchanged.
+#pragma unroll
+            for (int sw = 0; sw < 8; ++sw) s_pm[sw][tid] = 0u;
+            const uint32_t lo = __float_as_uint(r1.w), hi = __float_as_uint(r2.w);
+            const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
+            const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
+            if (x0 <= x1 && y0 <= y1) {
+                const int ty0 = ty * TILE_PIXELS;
+                const int sw0 = max((y0 - ty0) >> 1, 0), sw1 = min((y1 - ty0) >> 1, 7);  // floor halves
+                float rsx = 0.0f, rsy = 0.0f;
+                if (RECT) {
+                    rsx = 1.0f / (2.0f * r0.x);
+                    rsy = 1.0f / (2.0f * r0.w);
+                }
+                for (int sw = sw0; sw <= sw1; ++sw) {
+                    const int sy0 = ty0 + 2 * sw;  // the strip's first row
+                    int ca = x0 - wx0, cb = x1 - wx0;  // strip columns of the box
+                    if (RECT) {
+                        const float Xc = (float)(wx0 + 1), Yc = (float)(sy0 + 1);  // block 0's centre
+                        const float Xm = (float)(wx0 + 16), Ym = (float)(sy0 + 2);
+                        const float cx = fmaf(r0.y, Yc, fmaf(r0.x, Xc, r0.z));
+                        const float cy = fmaf(r1.x, Yc, fmaf(r0.w, Xc, r1.y));
+                        const float Tx = margin + 0.5f * (fabsf(r0.x) + fabsf(r0.y)) +
+                                         1e-6f * (fabsf(r0.x) * Xm + fabsf(r0.y) * Ym + fabsf(r0.z));
+                        const float Ty = margin + 0.5f * (fabsf(r0.w) + fabsf(r1.x)) +
+                                         1e-6f * (fabsf(r0.w) * Xm + fabsf(r1.x) * Ym + fabsf(r1.y));
+                        int lx, hx, ly, hy;
+                        g_interval(cx, 2.0f * r0.x, rsx, Tx, lx, hx);
+                        g_interval(cy, 2.0f * r0.w, rsy, Ty, ly, hy);
+                        ca = max(ca, 2 * max(lx, ly));
+                        cb = min(cb, 2 * min(hx, hy) + 1);
+                    }
+                    ca = max(ca, 0);
+                    cb = min(cb, 15);
+                    if (ca <= cb) {
+                        uint32_t pm = strip_columns_from(ca) & ~strip_columns_from(cb + 1);
+                        if (y0 > sy0) pm &= 0xCCCCCCCCu;      // lanes of the strip's second row
+                        if (y1 < sy0 + 1) pm &= 0x33333333u;  // lanes of its first row
+                        s_pm[sw][tid] = pm;
+                    }
+                }
+            }
         }
         __syncthreads();
         const uint32_t cnt = min((uint32_t)RASTER_BATCH, rg.y - b);
         if (!warp_done) {
-            // Per-pixel lists of the batch, 32 records per step.  Lane l tests record 32c + l against
-            // the warp's 2x16-pixel strip: the pixels inside the record's pixel box, and, for
-            // rectangles, only in the 2x2 blocks where some pixel centre may lie in the rectangle:
-            // over a block's four centres tc lies within tc(block centre) +- ext (half the block's
-            // extent mapped by |A|, widened by a rounding bound far above the per-pixel FMA chains'
-            // error), and along the strip the block centre's tc is c + 2g A, so |c + 2g A| <= margin +
-            // ext is an interval of block indices g.  Skipped pixels are not drawn by the record: the
-            // image is unchanged.  The 32 lane masks are transposed so that lane p holds word c of
-            // pixel p's list (bit i: record 32c + i), kept in s_plist; bit c of `nz` marks a non-empty
-            // word.
+            // Per-pixel lists of the batch, 32 records per step: the strip's lane masks of records
+            // 32c + l, transposed so that lane p holds word c of pixel p's list (bit i: record 32c + i),
+            // kept in s_plist; bit c of `nz` marks a non-empty word.
             uint32_t nz = 0u;
             for (uint32_t c = 0; c * 32u < cnt; ++c) {
-                uint32_t pm = 0u;
                 const uint32_t jl = c * 32u + lane;
-                if (jl < cnt) {
-                    const float4 r1 = s_q1[jl];
-                    const uint32_t lo = __float_as_uint(r1.w), hi = __float_as_uint(s_q2[jl].w);
-                    const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16);
-                    const int x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
-                    if (!(y1 < by0 || y0 > by0 + 1) && x0 <= x1) {
-                        int ca = x0 - wx0, cb = x1 - wx0;  // strip columns of the box
-                        if (RECT) {
-                            const float4 r0 = s_q0[jl];
-                            const float Xc = (float)(wx0 + 1), Yc = (float)(by0 + 1);  // block 0's centre
-                            const float Xm = (float)(wx0 + 16), Ym = (float)(by0 + 2);
-                            const float cx = fmaf(r0.y, Yc, fmaf(r0.x, Xc, r0.z));
-                            const float cy = fmaf(r1.x, Yc, fmaf(r0.w, Xc, r1.y));
-                            const float Tx = margin + 0.5f * (fabsf(r0.x) + fabsf(r0.y)) +
-                                             1e-6f * (fabsf(r0.x) * Xm + fabsf(r0.y) * Ym + fabsf(r0.z));
-                            const float Ty = margin + 0.5f * (fabsf(r0.w) + fabsf(r1.x)) +
-                                             1e-6f * (fabsf(r0.w) * Xm + fabsf(r1.x) * Ym + fabsf(r1.y));
-                            int lx, hx, ly, hy;
-                            g_interval(cx, 2.0f * r0.x, Tx, lx, hx);
-                            g_interval(cy, 2.0f * r0.w, Ty, ly, hy);
-                            ca = max(ca, 2 * max(lx, ly));
-                            cb = min(cb, 2 * min(hx, hy) + 1);
-                        }
-                        ca = max(ca, 0);
-                        cb = min(cb, 15);
-                        if (ca <= cb) {
-                            pm = strip_columns_from(ca) & ~strip_columns_from(cb + 1);
-                            if (y0 > by0) pm &= 0xCCCCCCCCu;      // lanes of the strip's second row
-                            if (y1 < by0 + 1) pm &= 0x33333333u;  // lanes of its first row
-                        }
-                    }
-                }
-                const uint32_t t = transpose_lane_bits(pm, lane);
+                const uint32_t pm = jl < cnt ? s_pm[w][jl] : 0u;
+                uint32_t t = 0u;
+                if (__any_sync(FULL_MASK, pm != 0u)) t = transpose_lane_bits(pm, lane);
                 s_plist[c][tid] = t;
                 nz |= (t != 0u ? 1u : 0u) << c;
             }

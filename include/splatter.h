@@ -157,6 +157,29 @@ SPL_API int spl_scene_load_chunk(spl_scene* s, const void* records, uint64_t sta
 SPL_API int spl_scene_load_chunk_file(spl_scene* s, const char* path, uint32_t header_bytes, uint64_t start, uint64_t count,
                               void* stream);
 
+/* A validating splat-file header parser (no reference counterpart; the reference reads such files
+ * unchecked, scene.rs:197-224): binary_little_endian 1.0 PLY, the vertex element first, exactly 62
+ * 32-bit float vertex properties (with check_names, in the standard order x y z nx ny nz f_dc_0..2
+ * f_rest_0..44 opacity scale_0..2 rot_0..3 — SerializedSplat, scene.rs:15-24), LF or CRLF lines, and
+ * a body of at least 248 bytes per declared splat.  Same outputs as spl_parse_file_header; every
+ * failure is SPL_ERR_IO with a message naming the line. */
+SPL_API int spl_validate_file_header(const char* path, int check_names, uint32_t* header_bytes, uint64_t* splat_count);
+
+/* Progressive loading as the reference's viewer does it (showcase.rs:13,54-59,98-103): a scene created
+ * for the file's full count is filled one chunk per step, the last chunk first, so frames rendered in
+ * between show the splats loaded so far (the others are still zero: no opacity, not drawn).
+ * chunk_size 0 loads the whole scene in the first step.  Each step reads its chunk into the pinned
+ * staging buffers and enqueues the copy and transform on `stream` (a frame rendered afterwards on
+ * that stream sees it); *chunks_left (may be NULL) receives the number of chunks still to load.  The
+ * file stays open until spl_progressive_loader_destroy.  (The reference's viewer also updates the
+ * host positions of its CPU sort at the chunk-relative index, scene.rs:259-261, so chunked loading
+ * with DepthSorting::Cpu sorts wrong positions there; here every mode reads the device arrays.) */
+typedef struct spl_progressive_loader spl_progressive_loader;
+SPL_API int spl_progressive_loader_create(spl_scene* s, const char* path, uint32_t header_bytes, uint64_t chunk_size,
+                                          spl_progressive_loader** out);
+SPL_API int spl_progressive_loader_step(spl_progressive_loader* l, void* stream, uint64_t* chunks_left);
+SPL_API void spl_progressive_loader_destroy(spl_progressive_loader* l);
+
 /* Writes splats already in the reference's device layout (60 floats: rotation[4], centre[3], pad,
  * scale[3], alpha, colourSH[48]; scene.rs:32, shaders.wgsl:28-35) from host memory — the write
  * new_dev_test does (scene.rs:178-182). */

@@ -4,7 +4,7 @@ The compute path is libsplatter_cuda.so (hand-written CUDA behind the C ABI in i
 this package is its Python host mirror of the reference's Renderer/Scene API.
 """
 from .renderer import (SORT_COOPERATIVE, SORT_ONESWEEP, BlendMode, Configuration, DepthSorting, FrameGraph,
-                       FrameInfo, Renderer, Scene, SplatterError, compute_uniforms)
+                       FrameInfo, ProgressiveLoader, Renderer, Scene, SplatterError, compute_uniforms)
 
-__all__ = ["BlendMode", "Configuration", "DepthSorting", "FrameGraph", "FrameInfo", "Renderer", "Scene",
-           "SplatterError", "compute_uniforms", "SORT_COOPERATIVE", "SORT_ONESWEEP"]
+__all__ = ["BlendMode", "Configuration", "DepthSorting", "FrameGraph", "FrameInfo", "ProgressiveLoader", "Renderer",
+           "Scene", "SplatterError", "compute_uniforms", "SORT_COOPERATIVE", "SORT_ONESWEEP"]

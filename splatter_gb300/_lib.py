@@ -119,6 +119,10 @@ SIGNATURES = [
     ("spl_scene_device_bytes", U64, [P]),
     ("spl_scene_create_dev_test", I32, [P, ctypes.POINTER(P)]),
     ("spl_parse_file_header", I32, [ctypes.c_char_p, ctypes.POINTER(U32), ctypes.POINTER(U64)]),
+    ("spl_validate_file_header", I32, [ctypes.c_char_p, I32, ctypes.POINTER(U32), ctypes.POINTER(U64)]),
+    ("spl_progressive_loader_create", I32, [P, ctypes.c_char_p, U32, U64, ctypes.POINTER(P)]),
+    ("spl_progressive_loader_step", I32, [P, P, ctypes.POINTER(U64)]),
+    ("spl_progressive_loader_destroy", None, [P]),
     ("spl_scene_load_chunk", I32, [P, P, U64, U64, P]),
     ("spl_scene_load_chunk_file", I32, [P, ctypes.c_char_p, U32, U64, U64, P]),
     ("spl_scene_write_splats", I32, [P, P, U64, U64, P]),

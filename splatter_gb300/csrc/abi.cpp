@@ -167,6 +167,24 @@ static int staged_upload(spl_scene* s, uint64_t start, uint64_t count, size_t it
     return SPL_OK;
 }
 
+// Splats [start, start + count) of a splat file open as `f`: seek to header + start * 248
+// (scene.rs:220-224), read through the pinned staging buffers, transform on the device.
+static int load_file_range(spl_scene* s, FILE* f, const char* path, uint32_t header_bytes, uint64_t start,
+                           uint64_t count, cudaStream_t st) {
+    if (std::fseek(f, (long)(header_bytes + start * 248ull), SEEK_SET) != 0)
+        return fail(SPL_ERR_IO, "seek failed in %s", path);
+    return staged_upload(
+        s, start, count, 62, st,
+        [&](float* dst, uint64_t, uint64_t cnt) {
+            if (std::fread(dst, 248, cnt, f) != cnt) return fail(SPL_ERR_IO, "short read in %s", path);
+            return SPL_OK;
+        },
+        [&](float* dev, uint64_t first, uint64_t cnt, cudaStream_t stm) {
+            launch_load_records(dev, (uint32_t)cnt, s->x + first, s->y + first, s->z + first, s->rot + first,
+                                s->scale_alpha + first, s->sh + first * 48, stm);
+        });
+}
+
 extern "C" {
 
 void spl_config_default(spl_config* cfg) {
@@ -674,22 +692,60 @@ int spl_scene_load_chunk_file(spl_scene* s, const char* path, uint32_t header_by
     if (count > s->n - start) count = s->n - start;
     FILE* f = std::fopen(path, "rb");
     if (!f) return fail(SPL_ERR_IO, "cannot open %s", path);
-    if (std::fseek(f, (long)(header_bytes + start * 248ull), SEEK_SET) != 0) {
-        std::fclose(f);
-        return fail(SPL_ERR_IO, "seek failed in %s", path);
-    }
-    int rc = staged_upload(
-        s, start, count, 62, (cudaStream_t)stream,
-        [&](float* dst, uint64_t, uint64_t cnt) {
-            if (std::fread(dst, 248, cnt, f) != cnt) return fail(SPL_ERR_IO, "short read in %s", path);
-            return SPL_OK;
-        },
-        [&](float* dev, uint64_t first, uint64_t cnt, cudaStream_t st) {
-            launch_load_records(dev, (uint32_t)cnt, s->x + first, s->y + first, s->z + first, s->rot + first,
-                                s->scale_alpha + first, s->sh + first * 48, st);
-        });
+    const int rc = load_file_range(s, f, path, header_bytes, start, count, (cudaStream_t)stream);
     std::fclose(f);
     return rc;
+}
+
+// ---- progressive loading (showcase.rs:13,54-59,98-103) ----------------------------------------------
+struct spl_progressive_loader {
+    spl_scene* s = nullptr;
+    FILE* f = nullptr;
+    std::string path;
+    uint32_t header_bytes = 0;
+    uint64_t chunk = 0;       // splats per step (0: the whole scene in one step)
+    uint64_t chunks_left = 0;
+};
+
+int spl_progressive_loader_create(spl_scene* s, const char* path, uint32_t header_bytes, uint64_t chunk_size,
+                                  spl_progressive_loader** out) {
+    if (!s || !path || !out) return fail(SPL_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    auto* l = new (std::nothrow) spl_progressive_loader();
+    if (!l) return fail(SPL_ERR_OOM, "host allocation failed");
+    l->f = std::fopen(path, "rb");
+    if (!l->f) {
+        delete l;
+        return fail(SPL_ERR_IO, "cannot open %s", path);
+    }
+    l->s = s;
+    l->path = path;
+    l->header_bytes = header_bytes;
+    l->chunk = chunk_size == 0 ? s->n : chunk_size;
+    l->chunks_left = l->chunk == 0 ? 0 : (s->n + l->chunk - 1) / l->chunk;  // showcase.rs:54-59
+    *out = l;
+    return SPL_OK;
+}
+
+int spl_progressive_loader_step(spl_progressive_loader* l, void* stream, uint64_t* chunks_left) {
+    if (!l) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (l->chunks_left > 0) {
+        // the last chunk not yet loaded (showcase.rs:98-101), clamped to the scene (scene.rs:217)
+        const uint64_t k = l->chunks_left - 1;
+        const uint64_t start = k * l->chunk;
+        const uint64_t count = std::min(l->chunk, l->s->n - start);
+        const int rc = load_file_range(l->s, l->f, l->path.c_str(), l->header_bytes, start, count, (cudaStream_t)stream);
+        if (rc) return rc;
+        l->chunks_left = k;
+    }
+    if (chunks_left) *chunks_left = l->chunks_left;
+    return SPL_OK;
+}
+
+void spl_progressive_loader_destroy(spl_progressive_loader* l) {
+    if (!l) return;
+    if (l->f) std::fclose(l->f);
+    delete l;
 }
 
 int spl_scene_write_splats(spl_scene* s, const float* splats60, uint64_t start, uint64_t count, void* stream) {

@@ -280,6 +280,25 @@ class Scene:
         check(lib.spl_parse_file_header(str(path).encode(), ctypes.byref(hb), ctypes.byref(n)))
         return int(hb.value), int(n.value)
 
+    @staticmethod
+    def validate_file_header(path, check_names=True):
+        """Validated header of a splat file: binary little-endian PLY with the vertex element first, 62
+        float vertex properties (in the standard order when check_names) and a body long enough for the
+        declared count; (header length in bytes, splat count), or SplatterError (SPL_ERR_IO)."""
+        lib = _lib.load()
+        hb = ctypes.c_uint32()
+        n = ctypes.c_uint64()
+        check(lib.spl_validate_file_header(str(path).encode(), 1 if check_names else 0, ctypes.byref(hb),
+                                           ctypes.byref(n)))
+        return int(hb.value), int(n.value)
+
+    @classmethod
+    def open_file(cls, renderer: Renderer, path, check_names=True):
+        """A scene for a splat file's full count (clamped to max_splat_count, scene.rs:46), its header
+        validated, nothing loaded yet: (scene, header length in bytes)."""
+        hb, n = cls.validate_file_header(path, check_names)
+        return cls(renderer, n), hb
+
     @property
     def handle(self):
         return self._h
@@ -334,3 +353,37 @@ class Scene:
         out = np.empty((count, 60), np.float32)
         check(self._lib.spl_scene_read_splats(self._h, out.ctypes.data_as(ctypes.c_void_p), int(start), int(count)))
         return out
+
+
+class ProgressiveLoader:
+    """Progressive loading as the reference's viewer does it (showcase.rs:13,54-59,98-103): each step
+    loads the last chunk not yet loaded, on the given stream, so frames rendered in between show the
+    splats loaded so far.  chunk_size 0 loads everything in the first step."""
+
+    def __init__(self, scene: Scene, path, header_bytes, chunk_size):
+        self._lib = _lib.load()
+        self.scene = scene
+        h = ctypes.c_void_p()
+        check(self._lib.spl_progressive_loader_create(scene.handle, str(path).encode(), int(header_bytes),
+                                                      int(chunk_size), ctypes.byref(h)))
+        self._h = h
+        n = scene.splat_count
+        self.chunks_left = 0 if n == 0 else (1 if chunk_size == 0 else (n + chunk_size - 1) // chunk_size)
+
+    def step(self, stream=None):
+        """Loads the next chunk (if any) on `stream`; returns the number of chunks still to load."""
+        left = ctypes.c_uint64()
+        check(self._lib.spl_progressive_loader_step(self._h, _stream_ptr(stream), ctypes.byref(left)))
+        self.chunks_left = int(left.value)
+        return self.chunks_left
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.spl_progressive_loader_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

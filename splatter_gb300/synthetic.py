@@ -130,3 +130,24 @@ def serving_scene_sizes(count=24, seed=3, lo=200_000, hi=6_000_000):
     """Splat counts of the serving configuration: log-uniform in [lo, hi]."""
     rng = np.random.default_rng(seed)
     return [int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) for _ in range(count)]
+
+
+def ply_property_names():
+    """The 62 vertex properties of a 3D-Gaussian splat file in record order (SerializedSplat,
+    scene.rs:15-24): centre, normal, 48 colour coefficients, opacity logit, log-scales, rotation."""
+    return (["x", "y", "z", "nx", "ny", "nz"] + [f"f_dc_{i}" for i in range(3)] + [f"f_rest_{i}" for i in range(45)] +
+            ["opacity"] + [f"scale_{i}" for i in range(3)] + [f"rot_{i}" for i in range(4)])
+
+
+def write_ply(path, records, crlf=False, comments=()):
+    """Writes (N, 62) float32 records as a binary little-endian PLY splat file; returns the header
+    length in bytes."""
+    rec = np.ascontiguousarray(records, dtype=np.float32).reshape(-1, 62)
+    nl = "\r\n" if crlf else "\n"
+    lines = ["ply", "format binary_little_endian 1.0", *[f"comment {c}" for c in comments],
+             f"element vertex {rec.shape[0]}", *[f"property float {p}" for p in ply_property_names()], "end_header"]
+    header = (nl.join(lines) + nl).encode()
+    with open(path, "wb") as f:
+        f.write(header)
+        f.write(rec.astype("<f4").tobytes())
+    return len(header)

@@ -114,6 +114,44 @@ def test_load_chunk_file(cuda, tmp_path):
     assert np.array_equal(s.read_splats(), t.read_splats())
 
 
+def test_progressive_loading_frames(cuda, tmp_path):
+    """The viewer's progressive loading (showcase.rs:54-59,98-103) from a validated file: after each
+    step the frame equals the oracle's frame of the scene with only the loaded chunks set (the others
+    zero, as in a fresh scene), and the last one equals the frame of the fully loaded scene."""
+    from splatter_gb300 import ProgressiveLoader
+    n, chunk, W, H = 60000, 16384, 320, 240
+    rec = synthetic.clustered(n, seed=21, sh_order=3)
+    p = tmp_path / "scene.ply"
+    hb = synthetic.write_ply(p, rec)
+    config = Configuration(max_splat_count=n, spherical_harmonics_order=3)
+    r = Renderer(config)
+    s, hb2 = Scene.open_file(r, p)
+    assert hb2 == hb and s.splat_count == n
+    loader = ProgressiveLoader(s, p, hb, chunk)
+    assert loader.chunks_left == 4
+    full = oracle.load_transform(rec)
+    part = {k: np.zeros_like(v) for k, v in full.items()}
+    cam = camera.look_at([4.0, 3.0, -34.0], [0.0, 0.0, 0.0])
+    u = oracle_uniforms(oracle, config, cam, W, H)
+    ocfg = oracle_cfg(oracle, config)
+    drawn = []
+    while loader.chunks_left:
+        left = loader.step()
+        lo, hi = left * chunk, min((left + 1) * chunk, n)  # the last chunk not yet loaded
+        for k in part:
+            part[k][lo:hi] = full[k][lo:hi]
+        img = r.render_frame(s, cam, W, H).cpu().numpy()
+        oimg, _ = oracle.render(u, ocfg, part, threads=THREADS)
+        assert np.array_equal(img, oimg)
+        drawn.append(int((img[..., 3] != 255).sum()))
+    assert drawn[0] > 0 and drawn[-1] > drawn[0]  # the picture fills in
+    assert loader.step() == 0  # nothing left: a no-op
+    t = Scene(r, n)
+    t.load_chunk(rec)
+    assert np.array_equal(r.render_frame(t, cam, W, H).cpu().numpy(), img)
+    loader.close()
+
+
 def test_dev_scene_matches_golden(cuda):
     import torch
     g = json.load(open(os.path.join(GOLDEN, "dev_scene.json")))

@@ -110,6 +110,25 @@ SPL_API int spl_renderer_reserve(spl_renderer* r, uint32_t width, uint32_t heigh
 SPL_API int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
                      uint32_t height, void* out_device, void* stream);
 
+/* ---- camera motors (renderer.rs:355-366, utils.rs:31-42) -------------------------------------------
+ * The reference's render_frame takes a projective-geometric-algebra motor.  Layout here (the crate
+ * geometric_algebra 0.3.0 that defines the reference's is not available; built from the algebra
+ * Cl(3,0,1) in double precision, rounded once to float):
+ *   motor  [s, e23, e31, e12, e01, e02, e03, e0123],  moving points by the sandwich M P ~M
+ *   rotor  [s, e23, e31, e12] ~ unit quaternion (w, x, y, z): a right-handed turn by 2 acos(s) about
+ *          the axis (e23, e31, e12) / sin, like showcase.rs:16-19's rotate_around_axis
+ * spl_motor_to_mat4 is motor3d_to_mat4: the images of the x, y, z directions and of the origin as
+ * columns (column-major), i.e. camera_to_world.  spl_motor_inverse is Motor::inverse
+ * (renderer.rs:365); spl_motor_product the geometric product (a applied after b);
+ * spl_motor_from_rotor_translation builds translator(t) * rotor (showcase.rs:140).
+ * spl_render_frame_motor renders with spl_motor_to_mat4 of the motor. */
+SPL_API int spl_motor_to_mat4(const float motor[8], float camera_to_world[16]);
+SPL_API int spl_motor_inverse(const float motor[8], float out[8]);
+SPL_API int spl_motor_product(const float a[8], const float b[8], float out[8]);
+SPL_API int spl_motor_from_rotor_translation(const float rotor[4], const float translation[3], float out[8]);
+SPL_API int spl_render_frame_motor(spl_renderer* r, const spl_scene* scene, const float motor[8], uint32_t width,
+                                   uint32_t height, void* out_device, void* stream);
+
 /* Waits for the renderer's last frame and returns its counters; returns SPL_ERR_LOOKBACK_TIMEOUT or
  * SPL_ERR_CAPACITY when the device flagged one. */
 SPL_API int spl_renderer_frame_info(spl_renderer* r, spl_frame_info* info);

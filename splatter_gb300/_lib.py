@@ -120,6 +120,11 @@ SIGNATURES = [
     ("spl_scene_create_dev_test", I32, [P, ctypes.POINTER(P)]),
     ("spl_parse_file_header", I32, [ctypes.c_char_p, ctypes.POINTER(U32), ctypes.POINTER(U64)]),
     ("spl_validate_file_header", I32, [ctypes.c_char_p, I32, ctypes.POINTER(U32), ctypes.POINTER(U64)]),
+    ("spl_motor_to_mat4", I32, [P, P]),
+    ("spl_motor_inverse", I32, [P, P]),
+    ("spl_motor_product", I32, [P, P, P]),
+    ("spl_motor_from_rotor_translation", I32, [P, P, P]),
+    ("spl_render_frame_motor", I32, [P, P, P, U32, U32, P, P]),
     ("spl_progressive_loader_create", I32, [P, ctypes.c_char_p, U32, U64, ctypes.POINTER(P)]),
     ("spl_progressive_loader_step", I32, [P, P, ctypes.POINTER(U64)]),
     ("spl_progressive_loader_destroy", None, [P]),

@@ -9,7 +9,7 @@ import math
 
 import numpy as np
 
-__all__ = ["look_at", "orbit_poses", "flythrough_poses", "rotor_translation_to_matrix"]
+__all__ = ["look_at", "orbit_poses", "flythrough_poses", "rotor_translation_to_matrix", "Motor"]
 
 
 def _normalize(v):
@@ -85,3 +85,51 @@ def flythrough_poses(n, seed, radius=(18.0, 32.0), jitter=6.0):
         tgt = rng.normal(0.0, jitter, 3)
         out.append(look_at(eye, tgt))
     return out
+
+
+class Motor:
+    """A camera motor of 3D projective geometric algebra, the reference's camera argument
+    (renderer.rs:355-366, showcase.rs:140): coefficients [s, e23, e31, e12, e01, e02, e03, e0123],
+    computed by the library's C functions (spl_motor_*)."""
+
+    def __init__(self, coefficients):
+        self.coefficients = np.ascontiguousarray(coefficients, dtype=np.float32).reshape(8).copy()
+
+    @staticmethod
+    def _call(fn, *arrays, n_out=8):
+        import ctypes
+        from . import _lib
+        out = np.empty(n_out, np.float32)
+        args = [np.ascontiguousarray(a, dtype=np.float32) for a in arrays]
+        _lib.check(getattr(_lib.load(), fn)(*[a.ctypes.data_as(ctypes.c_void_p) for a in args],
+                                            out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    @classmethod
+    def identity(cls):
+        return cls([1, 0, 0, 0, 0, 0, 0, 0])
+
+    @classmethod
+    def from_rotor_translation(cls, rotor, translation):
+        """translator(translation) * rotor, the rotor [s, e23, e31, e12] a unit quaternion (w, x, y, z)."""
+        return cls(cls._call("spl_motor_from_rotor_translation", np.asarray(rotor, np.float32).reshape(4),
+                             np.asarray(translation, np.float32).reshape(3)))
+
+    @staticmethod
+    def rotate_around_axis(angle, axis):
+        """The rotor of a right-handed turn by `angle` about the unit `axis` (showcase.rs:16-19)."""
+        h = 0.5 * float(angle)
+        return np.array([math.cos(h), axis[0] * math.sin(h), axis[1] * math.sin(h), axis[2] * math.sin(h)],
+                        np.float32)
+
+    def matrix(self):
+        """motor3d_to_mat4 (utils.rs:31-42): camera-to-world, column-major float32[16]."""
+        return self._call("spl_motor_to_mat4", self.coefficients, n_out=16)
+
+    def inverse(self):
+        """Motor::inverse (renderer.rs:365)."""
+        return Motor(self._call("spl_motor_inverse", self.coefficients))
+
+    def __mul__(self, other):
+        """Geometric product: self applied after other."""
+        return Motor(self._call("spl_motor_product", self.coefficients, other.coefficients))

@@ -387,6 +387,15 @@ static int render_frame_impl(spl_renderer* r, const SceneView& sv, const Uniform
     return SPL_OK;
 }
 
+int spl_render_frame_motor(spl_renderer* r, const spl_scene* scene, const float motor[8], uint32_t width,
+                           uint32_t height, void* out_device, void* stream) {
+    if (!motor) return fail(SPL_ERR_INVALID, "NULL argument");
+    float cam[16];
+    const int rc = spl_motor_to_mat4(motor, cam);  // renderer.rs:364
+    if (rc) return rc;
+    return spl_render_frame(r, scene, cam, width, height, out_device, stream);
+}
+
 int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
                      uint32_t height, void* out_device, void* stream) {
     if (!r || !scene || !camera_to_world || !out_device) return fail(SPL_ERR_INVALID, "NULL argument");

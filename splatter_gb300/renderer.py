@@ -150,6 +150,16 @@ class Renderer:
                                          int(height), ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream)))
         return out
 
+    def render_frame_motor(self, scene, motor, width, height, out=None, stream=None):
+        """render_frame with the reference's camera argument, a PGA motor (renderer.rs:355-364):
+        8 floats [s, e23, e31, e12, e01, e02, e03, e0123] or a camera.Motor."""
+        if out is None:
+            out = self.output_buffer(width, height)
+        m = np.ascontiguousarray(getattr(motor, "coefficients", motor), dtype=np.float32).reshape(8)
+        check(self._lib.spl_render_frame_motor(self._h, scene.handle, m.ctypes.data_as(ctypes.c_void_p), int(width),
+                                               int(height), ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream)))
+        return out
+
     def render_frame_ptr(self, scene, camera_to_world, width, height, out_ptr, stream_ptr):
         """Raw-pointer variant (device output pointer and cudaStream_t as ints)."""
         cam = _cam(camera_to_world)

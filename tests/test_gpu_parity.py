@@ -152,6 +152,25 @@ def test_progressive_loading_frames(cuda, tmp_path):
     loader.close()
 
 
+def test_render_frame_motor(cuda):
+    """The reference's camera argument (a PGA motor, renderer.rs:355-364): the frame equals the frame
+    of its motor3d_to_mat4 matrix and the oracle's frame of that camera."""
+    from splatter_gb300.camera import Motor
+    n, W, H = 20000, 256, 192
+    rec = synthetic.clustered(n, seed=31, sh_order=3)
+    config = Configuration(max_splat_count=n, spherical_harmonics_order=3)
+    r = Renderer(config)
+    s = Scene(r, n)
+    s.load_chunk(rec)
+    m = Motor.from_rotor_translation(Motor.rotate_around_axis(0.3, (0.0, 1.0, 0.0)), (-9.0, 1.0, -28.0))
+    img = r.render_frame_motor(s, m, W, H).cpu().numpy()
+    assert np.array_equal(img, r.render_frame(s, m.matrix(), W, H).cpu().numpy())
+    oimg, _ = oracle.render(oracle_uniforms(oracle, config, m.matrix(), W, H), oracle_cfg(oracle, config),
+                            oracle.load_transform(rec), threads=THREADS)
+    assert np.array_equal(img, oimg)
+    assert int((img[..., 3] != 255).sum()) > 100
+
+
 def test_dev_scene_matches_golden(cuda):
     import torch
     g = json.load(open(os.path.join(GOLDEN, "dev_scene.json")))

@@ -55,6 +55,7 @@ def parse_args(argv=None):
     p.add_argument("--no-differentiation", action="store_true", help="skip the forward+backward leg")
     p.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain leg")
     p.add_argument("--no-uhd", action="store_true", help="skip the 3840x2160 measurement")
+    p.add_argument("--no-loading", action="store_true", help="skip the splat-file loading leg")
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-requests", type=int, default=800, help="closed-loop requests per loop")
     p.add_argument("--serve-rates", default="250,1000,2000", help="Poisson arrival rates (req/s)")
@@ -410,6 +411,10 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_differentiation:
         diff = run_differentiation(args)
 
+    loading = None
+    if rank == 0 and world == 1 and not args.no_loading:
+        loading = run_loading(args)
+
     serving = None
     if rank == 0 and world == 1 and not args.no_serving:
         del s, r, out
@@ -428,7 +433,7 @@ def run_ours(args):
             "config": bench_config(args, world, vis_tot / frames_prof),
             "splats_per_s": round(value * args.splats, 0),
             "stages": stages, "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-            "cpu_baseline": cpu, "uhd": uhd, "differentiation": diff, "serving": serving,
+            "cpu_baseline": cpu, "uhd": uhd, "differentiation": diff, "loading": loading, "serving": serving,
         }
         s_line = json.dumps(line)
         print(s_line, flush=True)
@@ -443,6 +448,56 @@ def run_ours(args):
 DIFF_WORKLOAD = ("1M splats, SH degree 3, clustered, 1024x1024, 8 orbit views; targets from the seed scene, "
                  "forward on a copy with positions + N(0, 0.01^2), log-scales + N(0, 0.05^2), opacity logits + "
                  "N(0, 0.2^2); L2 image loss; fp32 blend")
+
+
+def run_loading(args, n=1_000_000, chunk=32768, W=1920, H=1080):
+    """Splat-file loading: a validated 1M-splat PLY (248 MB, written to a temporary directory, so read
+    back through the page cache) loaded whole through the pinned staging buffers, and the viewer's
+    progressive loading (showcase.rs:13,98-103): one 32k-splat chunk before each 1080p frame."""
+    import torch
+    from splatter_gb300 import Configuration, ProgressiveLoader, Renderer, Scene, camera, synthetic
+    rec = synthetic.clustered(n, seed=args.seed + 17, sh_order=3)
+    stream = torch.cuda.current_stream()
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "scene.ply")
+        synthetic.write_ply(path, rec)
+        del rec
+        r = Renderer(Configuration(max_splat_count=n, spherical_harmonics_order=3,
+                                   field_of_view_y=math.radians(60.0)))
+        whole = Scene(r, n)
+        t_hdr, t_load = [], []
+        for _ in range(4):
+            t0 = time.perf_counter()
+            hb, cnt = Scene.validate_file_header(path)
+            t1 = time.perf_counter()
+            whole.load_chunk_file(path, hb, 0, cnt, stream)
+            torch.cuda.synchronize()
+            t_hdr.append(t1 - t0)
+            t_load.append(time.perf_counter() - t1)
+        load_s = min(t_load[1:])
+        poses = camera.orbit_poses(64, args.seed + 19, radius=(30.0, 45.0))
+        out = r.output_buffer(W, H)
+        prog = Scene(r, n)
+        loader = ProgressiveLoader(prog, path, hb, chunk)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        frames = 0
+        while loader.chunks_left:
+            loader.step(stream)
+            r.render_frame(prog, poses[frames % len(poses)], W, H, out=out, stream=stream)
+            frames += 1
+        torch.cuda.synchronize()
+        prog_s = time.perf_counter() - t0
+        same = bool(torch.equal(r.render_frame(prog, poses[1], W, H), r.render_frame(whole, poses[1], W, H)))
+        loader.close()
+    return {"workload": f"{n} splats (clustered, SH 3) in a {248 * n / 1e6:.0f} MB binary PLY read through the page "
+                        f"cache; progressive: {chunk}-splat chunks, one before each {W}x{H} frame",
+            "header_validation_ms": round(1000.0 * min(t_hdr), 3),
+            "whole_file_load_ms": round(1000.0 * load_s, 2),
+            "whole_file_gb_per_s": round(248.0 * n / load_s / 1e9, 2),
+            "progressive_chunks": frames, "progressive_total_ms": round(1000.0 * prog_s, 2),
+            "progressive_frames_per_s": round(frames / prog_s, 1),
+            "progressive_result_equals_whole_load": same}
 
 
 def run_differentiation(args, iters=5, warmup=3):

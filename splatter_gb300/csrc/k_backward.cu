@@ -239,8 +239,9 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
         const float rx = Xr * ((2.0f * vw) / (float)u.image_size[0]) - vw;
         const float ry = vh - Yr * ((2.0f * vh) / (float)u.image_size[1]);
         float gin[10];
+        // centre directions: geometry and colour (the view direction moves with the centre)
 #pragma unroll 1
-        for (int dir = 0; dir < 10; ++dir) {
+        for (int dir = 0; dir < 3; ++dir) {
             Df d[10];
 #pragma unroll
             for (int k = 0; k < 10; ++k) d[k] = Df{in[k], k == dir ? 1.0f : 0.0f};
@@ -250,6 +251,19 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
             float acc = (g[0] * o.A00.d + g[1] * o.A01.d) + (g[2] * o.B0r.d + g[3] * o.A10.d);
             acc += (g[4] * o.A11.d + g[5] * o.B1r.d);
             acc += (g[7] * o.cr.d + g[8] * o.cg.d) + g[9] * o.cb.d;
+            gin[dir] = isfinite(acc) ? acc : 0.0f;
+        }
+        // rotation and scale directions: the colour does not depend on them
+#pragma unroll 1
+        for (int dir = 3; dir < 10; ++dir) {
+            Df d[10];
+#pragma unroll
+            for (int k = 0; k < 10; ++k) d[k] = Df{in[k], k == dir ? 1.0f : 0.0f};
+            VertexOut<Df> o;
+            vertex_math<SHO, COV, Df, true, false>(u, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], sh,
+                                                   o, rx, ry);
+            float acc = (g[0] * o.A00.d + g[1] * o.A01.d) + (g[2] * o.B0r.d + g[3] * o.A10.d);
+            acc += (g[4] * o.A11.d + g[5] * o.B1r.d);
             gin[dir] = isfinite(acc) ? acc : 0.0f;
         }
         gx[i] = gin[0];

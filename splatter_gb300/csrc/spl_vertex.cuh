@@ -373,18 +373,24 @@ struct VertexOut {
 // (rx, ry), computed from the small offset (rx - t0, ry - t1).  The backward differentiates
 // tc = A (X - Xr, Y - Yr) + Br instead of A (X, Y) + B: the same function, but without the large,
 // cancelling terms that absolute pixel coordinates put into dB/dp.
-template <int SHO, bool COV, class S, bool REF = false>
+// Without COLOUR the colour is left out (o.cr, o.cg, o.cb zero): the backward's rotation and scale
+// directions, on which the colour does not depend.
+template <int SHO, bool COV, class S, bool REF = false, bool COLOUR = true>
 __device__ __forceinline__ void vertex_math(const Uniforms& u, S cx, S cy, S cz, S q0, S q1, S q2, S q3, S scx, S scy,
                                             S scz, const float* sh, VertexOut<S>& o, float rx = 0.0f,
                                             float ry = 0.0f) {
-    // colour (shaders.wgsl:531-532)
-    const S vx = cx - u.camera[12], vy = cy - u.camera[13], vz = cz - u.camera[14];
-    const S len = sqrt_((vx * vx + vy * vy) + vz * vz);
-    const S dx = vx / len, dy = vy / len, dz = vz / len;
-    const S dxx = dx * dx, dyy = dy * dy, dzz = dz * dz;
-    o.cr = sh_channel<SHO>(sh, 0, dx, dy, dz, dxx, dyy, dzz);
-    o.cg = sh_channel<SHO>(sh, 1, dx, dy, dz, dxx, dyy, dzz);
-    o.cb = sh_channel<SHO>(sh, 2, dx, dy, dz, dxx, dyy, dzz);
+    if constexpr (COLOUR) {
+        // colour (shaders.wgsl:531-532)
+        const S vx = cx - u.camera[12], vy = cy - u.camera[13], vz = cz - u.camera[14];
+        const S len = sqrt_((vx * vx + vy * vy) + vz * vz);
+        const S dx = vx / len, dy = vy / len, dz = vz / len;
+        const S dxx = dx * dx, dyy = dy * dy, dzz = dz * dz;
+        o.cr = sh_channel<SHO>(sh, 0, dx, dy, dz, dxx, dyy, dzz);
+        o.cg = sh_channel<SHO>(sh, 1, dx, dy, dz, dxx, dyy, dzz);
+        o.cb = sh_channel<SHO>(sh, 2, dx, dy, dz, dxx, dyy, dzz);
+    } else {
+        o.cr = o.cg = o.cb = cst<S>(0.0f);
+    }
     // conic + decomposition (shaders.wgsl:533-542)
     const S sx = scx * u.splat_scale, sy = scy * u.splat_scale, sz = scz * u.splat_scale;
     S t0, t1, rj, rk, ax0, ax1;

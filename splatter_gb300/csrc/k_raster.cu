@@ -18,6 +18,7 @@
 namespace spl {
 
 // ------------------------------------------------------------------------------------------------
+constexpr int BIN_PER = BIN_TILE / 256;  // consecutive draw entries per thread (thread order = depth order)
 template <bool ORDERED, bool HIST>
 __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order, const uint2* __restrict__ boxes,
                                              FrameCounters* fc, int mode, const uint32_t* __restrict__ epoch_word,
@@ -28,6 +29,7 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
     __shared__ uint32_t s_slot[BIN_TILE];
     __shared__ uint32_t s_box[BIN_TILE];  // tx0 | ty0 << 16
     __shared__ uint16_t s_bw[BIN_TILE];
+    __shared__ uint32_t s_map[1024];  // emission step: entry + 1 at each entry's first pair position
     __shared__ uint32_t s_hist[HIST ? 768 : 1];
     __shared__ uint32_t s_scan[8];
     __shared__ uint32_t s_tile, s_epoch, s_base, s_draw;
@@ -58,10 +60,10 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
     }
     if (tile == 0 && tid == 0) fc->draw = draw;
     // per-entry tile counts (4 consecutive entries per thread keep the thread order = depth order)
-    uint32_t cnt[4], tsum = 0;
+    uint32_t cnt[BIN_PER], tsum = 0;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const uint32_t r = tile * BIN_TILE + tid * 4u + e;
+    for (int e = 0; e < BIN_PER; ++e) {
+        const uint32_t r = tile * BIN_TILE + tid * (uint32_t)BIN_PER + e;
         uint32_t c = 0, slot = 0, box = 0, bw = 0;
         if (r < draw) {
             slot = ORDERED ? __ldg(order + r) : r;
@@ -77,16 +79,16 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
             }
         }
         cnt[e] = c;
-        s_slot[tid * 4 + e] = slot;
-        s_box[tid * 4 + e] = box;
-        s_bw[tid * 4 + e] = (uint16_t)bw;
+        s_slot[tid * BIN_PER + e] = slot;
+        s_box[tid * BIN_PER + e] = box;
+        s_bw[tid * BIN_PER + e] = (uint16_t)bw;
         tsum += c;
     }
     uint32_t btot;
     uint32_t off = block_exclusive_scan_256(tsum, s_scan, &btot);
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        s_off[tid * 4 + e] = off;
+    for (int e = 0; e < BIN_PER; ++e) {
+        s_off[tid * BIN_PER + e] = off;
         off += cnt[e];
     }
     if (tid < 32) {
@@ -103,28 +105,76 @@ __global__ void __launch_bounds__(256) k_bin(const uint32_t* __restrict__ order,
     }
     __syncthreads();
     const uint32_t gbase = s_base;
-    // load-balanced emission: pair q of this CTA belongs to the last entry whose offset <= q
-    for (uint32_t q = tid; q < btot; q += 256u) {
-        uint32_t lo = 0, hi = BIN_TILE;  // find largest e with s_off[e] <= q (entries with c == 0 share offsets)
-        while (hi - lo > 1u) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_off[mid] <= q) lo = mid;
-            else hi = mid;
+    // Load-balanced emission, 1024 pairs per step: pair q of this CTA belongs to the last entry whose
+    // offset is <= q.  Each entry with pairs marks its first pair's position (entry + 1), and an
+    // inclusive max-scan over the step's positions (carrying the previous step's last entry) hands
+    // every position its entry; thread t emits positions 4t .. 4t + 3.
+    uint32_t carry = 0u;
+    for (uint32_t q0 = 0; q0 < btot; q0 += 1024u) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s_map[tid * 4 + k] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < BIN_PER; ++e) {
+            const uint32_t ei = tid * (uint32_t)BIN_PER + e;
+            const uint32_t o = s_off[ei];
+            if (cnt[e] != 0u && o >= q0 && o - q0 < 1024u) s_map[o - q0] = ei + 1u;
         }
-        const uint32_t li = q - s_off[lo];
-        const uint32_t bw = s_bw[lo], box = s_box[lo];
-        const uint32_t ty = (box >> 16) + li / bw, tx = (box & 0xFFFFu) + li % bw;
-        const uint32_t tid_tile = ty * (uint32_t)tiles_x + tx;
-        const uint32_t g = gbase + q;
-        if (g < pair_cap) {
-            pair_keys[g] = tid_tile;
-            pair_vals[g] = s_slot[lo];
-            if (HIST) {
-                atomicAdd(&s_hist[tid_tile & 255u], 1u);
-                atomicAdd(&s_hist[256u + ((tid_tile >> 8) & 255u)], 1u);
-                atomicAdd(&s_hist[512u + ((tid_tile >> 16) & 255u)], 1u);
+        __syncthreads();
+        uint32_t v[4], m = carry;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            m = max(m, s_map[tid * 4 + k]);
+            v[k] = m;  // thread-local inclusive max (with the carry)
+        }
+        uint32_t x = m;  // inclusive max-scan of the thread maxima over the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
+            if ((tid & 31u) >= (uint32_t)o) x = max(x, y);
+        }
+        const uint32_t before_in_warp = __shfl_up_sync(FULL_MASK, x, 1);
+        if ((tid & 31u) == 31u) s_scan[tid >> 5] = x;
+        __syncthreads();
+        uint32_t before = (tid & 31u) ? before_in_warp : 0u, all = 0u;
+#pragma unroll
+        for (uint32_t wi = 0; wi < 8; ++wi) {
+            const uint32_t sw = s_scan[wi];
+            before = wi < (tid >> 5) ? max(before, sw) : before;
+            all = max(all, sw);
+        }
+        carry = all;  // the entry at the step's last position: the carry into the next step
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t q = q0 + tid * 4u + k;
+            const uint32_t marked = max(before, v[k]);  // >= 1: position 0 of the first step is marked
+            if (q >= btot || marked == 0u) break;
+            const uint32_t e = marked - 1u;
+            const uint32_t li = q - s_off[e];
+            const uint32_t bw = s_bw[e], box = s_box[e];
+            // li / bw and li % bw (li < 2^24): float estimate, corrected by one step
+            uint32_t dy = __float2uint_rz(__fdividef((float)li, (float)bw));
+            int32_t dx = (int32_t)(li - dy * bw);
+            if (dx < 0) {
+                --dy;
+                dx += (int32_t)bw;
+            } else if (dx >= (int32_t)bw) {
+                ++dy;
+                dx -= (int32_t)bw;
+            }
+            const uint32_t tid_tile = ((box >> 16) + dy) * (uint32_t)tiles_x + (box & 0xFFFFu) + (uint32_t)dx;
+            const uint32_t g = gbase + q;
+            if (g < pair_cap) {
+                pair_keys[g] = tid_tile;
+                pair_vals[g] = s_slot[e];
+                if (HIST) {
+                    atomicAdd(&s_hist[tid_tile & 255u], 1u);
+                    atomicAdd(&s_hist[256u + ((tid_tile >> 8) & 255u)], 1u);
+                    atomicAdd(&s_hist[512u + ((tid_tile >> 16) & 255u)], 1u);
+                }
             }
         }
+        __syncthreads();  // s_map and s_scan are rewritten by the next step
     }
     if (HIST) {
         __syncthreads();

@@ -1,7 +1,7 @@
 // Onesweep LSD radix sort pass (sm_103a), the GPU depth sort of splatter (radixSortB/radixSortC,
 // Lichtso/splatter src/shaders.wgsl:338-498) rebuilt for CUDA:
-//   * warp-level multisplit ranking with __match_any_sync (the reference ranks with shared atomics
-//     because WebGPU has no subgroup ops, shaders.wgsl:428-429), which makes every pass STABLE;
+//   * warp-level multisplit ranking (digit match by eight ballots; the reference ranks with shared
+//     atomics because WebGPU has no subgroup ops, shaders.wgsl:428-429), which makes every pass STABLE;
 //   * one CTA of 256 threads ranks a tile of 4096 keys (16 per thread, warp-striped, so global loads
 //     are coalesced and the warp order is the input order);
 //   * the global digit offsets come from the digit histogram computed upstream (the reference's
@@ -50,19 +50,20 @@ __global__ void __launch_bounds__(OS_THREADS, 3)
         if (tile >= ntiles) break;
         const uint32_t tbase = tile * SORT_TILE;
         const uint32_t base = tbase + w * 512u + lane;
-        uint32_t key[OS_KPT], pos[OS_KPT];
+        uint32_t key[OS_KPT], pos[OS_KPT], val[OS_KPT];
 #pragma unroll
         for (int j = 0; j < OS_KPT; ++j) {
             const uint32_t e = base + 32u * j;
             key[j] = e < n ? __ldg(keys_in + e) : 0u;
+            val[j] = e < n ? (IOTA ? e : __ldg(vals_in + e)) : 0u;  // loaded with the keys
         }
         // warp-level multisplit: rank of each key among equal digits of its warp, in input order
 #pragma unroll
         for (int j = 0; j < OS_KPT; ++j) {
             const uint32_t e = base + 32u * j;
             const bool valid = e < n;
-            const uint32_t d = valid ? (key[j] >> shift) & 255u : 256u;
-            const uint32_t peers = __match_any_sync(FULL_MASK, d);
+            const uint32_t d = (key[j] >> shift) & 255u;
+            const uint32_t peers = match_digit(d, valid);
             uint32_t cnt = 0;
             if (valid) cnt = s_whist[w][d];
             __syncwarp();
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(OS_THREADS, 3)
 #pragma unroll
         for (int j = 0; j < OS_KPT; ++j) {
             const uint32_t e = base + 32u * j;
-            if (e < n) s_buf[pos[j]] = IOTA ? e : __ldg(vals_in + e);
+            if (e < n) s_buf[pos[j]] = val[j];
         }
         __syncthreads();
 #pragma unroll

@@ -38,19 +38,6 @@ struct CoopSmem {
     uint32_t scan[CS_WARPS];
 };
 
-// Lanes whose 8-bit digit equals this lane's (valid lanes only), from eight ballots: the warp-level
-// multisplit match without MATCH.ANY, whose latency dominated the ranking.
-__device__ __forceinline__ uint32_t match_digit(uint32_t d, bool valid) {
-    uint32_t peers = __ballot_sync(FULL_MASK, valid);
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-        const bool bit = (d >> b) & 1u;
-        const uint32_t m = __ballot_sync(FULL_MASK, bit);
-        peers &= bit ? m : ~m;
-    }
-    return peers;
-}
-
 __device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t spin_limit, uint32_t* err) {
     __syncthreads();
     if (threadIdx.x == 0) {

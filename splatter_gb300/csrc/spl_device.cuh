@@ -176,6 +176,19 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Lanes whose 8-bit digit equals this lane's (valid lanes only), from eight ballots: the warp-level
+// multisplit match without MATCH.ANY, whose latency dominated the ranking.
+__device__ __forceinline__ uint32_t match_digit(uint32_t d, bool valid) {
+    uint32_t peers = __ballot_sync(FULL_MASK, valid);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t m = __ballot_sync(FULL_MASK, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
+
 // Block-wide exclusive scan of one u32 per thread (blockDim.x == 256).  `scratch` holds 8 words.
 __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_t* scratch, uint32_t* total) {
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;

@@ -5,8 +5,9 @@
 // so the frame is tiled into 16x16-pixel tiles:
 //   k_bin          - for each drawn entry in depth order, the tiles its pixel box touches; emitted as
 //                    (tile id, record slot) pairs at offsets from a decoupled look-back scan, with
-//                    load-balanced emission inside the CTA and the tile-id digit histograms
-//   (2 onesweep passes over the 16-bit tile ids: stable, so each tile's list stays in depth order)
+//                    load-balanced emission inside the CTA (a max-scan over the entries' first
+//                    pairs) and, for the onesweep sort, the tile-id digit histograms
+//   (a stable radix sort of the pairs by tile id, so each tile's list stays in depth order)
 //   k_tile_ranges  - start/end of each tile's run in the sorted pair list
 //   k_tile_order   - the raster's tile order: most pairs first
 //   k_raster       - one CTA per tile, one thread per pixel; records staged through shared memory in

@@ -238,6 +238,9 @@ def load_peaks():
 # its own frames by their pair counts.
 TRAFFIC_PER_UNIT = {"raster": {"per_pair": 242.7e6 / 3353969.0, "per_launch": 7.2e6,
                                "source": "profiles/k_raster_3m_1080p.md (3M-splat capture, scaled by pairs)"}}
+# The raster is bound by instruction issue, not HBM: the fraction of issue slots its warps used in the
+# same capture (smsp__issue_active, pct of peak, active), reported beside the HBM figure.
+ISSUE_ACTIVE = {"raster": {"frac": 0.855, "source": "profiles/k_raster_3m_1080p.md smsp__issue_active"}}
 
 
 def stage_traffic(stage, P):
@@ -354,6 +357,9 @@ def run_ours(args):
                 "unit": "GB/s", "frac": stages[dominant]["frac"], "peak_kind": f"{peak_kind} hbm_gbs",
                 "traffic": traffic, "traffic_source": TRAFFIC_PER_UNIT.get(dominant, {}).get("source"),
                 "algorithmic_bytes_per_launch": int(stage_bytes_sum[dominant] / frames_prof)}
+    if dominant in ISSUE_ACTIVE:
+        roofline["sm_issue_active_frac"] = ISSUE_ACTIVE[dominant]["frac"]
+        roofline["sm_issue_active_source"] = ISSUE_ACTIVE[dominant]["source"]
 
     # ---- end to end through the public API with host buffers ----
     # Two output buffers and two streams: frame k+1 renders while frame k's image travels to the host

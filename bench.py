@@ -351,6 +351,10 @@ def run_ours(args):
         avg_ms = stage_ms[name] / frames_prof
         gbs = stage_bytes_sum[name] / (stage_ms[name] / 1000.0) / 1e9 if stage_ms[name] > 0 else 0.0
         stages[name] = {"ms": round(avg_ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
+    # sorted keys per second (all passes of a sort count once per key)
+    for name, keys in (("depth_sort", vis_tot), ("pair_sort", pairs_tot)):
+        if name in stages and stage_ms[name] > 0:
+            stages[name]["keys_per_s"] = round(keys / (stage_ms[name] / 1000.0), 0)
     dominant = max(stages, key=lambda n: stages[n]["ms"])
     traffic = stage_traffic(dominant, pairs_tot / frames_prof)
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": stages[dominant]["gbs"], "peak": peak,

@@ -152,6 +152,33 @@ def test_progressive_loading_frames(cuda, tmp_path):
     loader.close()
 
 
+@pytest.mark.parametrize("chunk", [0, 7000, 50000])
+def test_progressive_loader_edge_cases(cuda, tmp_path, chunk):
+    """chunk 0 (everything in the first step), a chunk that does not divide the count, a chunk above
+    the count; and a file larger than max_splat_count (the scene clamps, scene.rs:46): every step
+    count and the final scene equal a whole load of the same (clamped) range."""
+    from splatter_gb300 import ProgressiveLoader
+    n_file, n_max = 23000, 20000
+    rec = synthetic.plain_small(n_file, seed=41, sh_order=3)
+    p = tmp_path / "s.ply"
+    hb = synthetic.write_ply(p, rec)
+    r = Renderer(Configuration(max_splat_count=n_max, spherical_harmonics_order=3))
+    s, hb2 = Scene.open_file(r, p)
+    assert hb2 == hb and s.splat_count == n_max
+    loader = ProgressiveLoader(s, p, hb, chunk)
+    want_steps = 1 if chunk == 0 else -(-n_max // chunk)
+    assert loader.chunks_left == want_steps
+    steps = 0
+    while loader.chunks_left:
+        loader.step()
+        steps += 1
+    assert steps == want_steps and loader.step() == 0
+    t = Scene(r, n_max)
+    t.load_chunk(rec[:n_max])
+    assert np.array_equal(s.read_splats(), t.read_splats())
+    loader.close()
+
+
 def test_render_frame_motor(cuda):
     """The reference's camera argument (a PGA motor, renderer.rs:355-364): the frame equals the frame
     of its motor3d_to_mat4 matrix and the oracle's frame of that camera."""

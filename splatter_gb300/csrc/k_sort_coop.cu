@@ -26,6 +26,7 @@ constexpr int CS_NQ = CS_THREADS / 256;        // threads per digit in the per-d
 constexpr int CS_WPQ = CS_WARPS / CS_NQ;       // warps summed by one of those threads
 constexpr int CS_KPT = 8;
 constexpr int CS_TILE = CS_THREADS * CS_KPT;  // 4096 keys per sub-tile
+static_assert(CS_THREADS % 256 == 0, "the per-digit phases map 256 digits onto groups of threads");
 
 struct CoopSmem {
     uint32_t buf[CS_TILE];             // staging for keys, then values
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
             for (int k = 0; k < 8; ++k) sm.wcnt[w][lane + 32 * k] = 0u;
             __syncwarp();
             uint32_t key[CS_KPT], pos[CS_KPT], val[CS_KPT];
-            const uint32_t wb = tb + w * 256u + lane;
+            const uint32_t wb = tb + w * (32u * CS_KPT) + lane;  // warp w owns 32 x CS_KPT consecutive keys
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
                 const uint32_t e = wb + 32u * j;

@@ -199,10 +199,33 @@ void launch_bin(int mode, bool hist, const uint32_t* order, const uint2* boxes, 
 __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const FrameCounters* __restrict__ fc,
                               uint32_t pair_cap, uint2* ranges) {
     const uint32_t P = min(fc->pairs, pair_cap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
-        const uint32_t k = keys[i];
-        if (i == 0 || keys[i - 1] != k) ranges[k].x = i;
-        if (i + 1 == P || keys[i + 1] != k) ranges[k].y = i + 1;
+    // four keys per thread (one 16-byte load; the neighbours across the group edges loaded singly)
+    const uint32_t groups = (P + 3u) / 4u;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x) {
+        const uint32_t i0 = g * 4u;
+        uint32_t k[4];
+        if (i0 + 4u <= P) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(keys + i0));
+            k[0] = v.x;
+            k[1] = v.y;
+            k[2] = v.z;
+            k[3] = v.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) k[j] = i0 + j < P ? __ldg(keys + i0 + j) : 0u;
+        }
+        const bool has_prev = i0 > 0u, has_next = i0 + 4u < P;
+        const uint32_t prev = has_prev ? __ldg(keys + i0 - 1u) : 0u;
+        const uint32_t next = has_next ? __ldg(keys + i0 + 4u) : 0u;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = i0 + j;
+            if (i >= P) break;
+            const bool starts = j > 0 ? k[j - 1] != k[j] : (!has_prev || prev != k[j]);
+            const bool ends = i + 1u == P || (j < 3 ? k[j + 1] != k[j] : next != k[j]);
+            if (starts) ranges[k[j]].x = i;
+            if (ends) ranges[k[j]].y = i + 1u;
+        }
     }
 }
 

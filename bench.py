@@ -535,13 +535,16 @@ def run_loading(args, n=1_000_000, chunk=32768, W=1920, H=1080):
 
 
 def run_differentiation(args, iters=5, warmup=3):
-    """Forward+backward ms/iter through torch.autograd (render_raw: the loader's activations in torch,
-    the hand-written backward behind the autograd Function).  One iteration = the 8 views, each
-    rendered, compared with its target and back-propagated (gradients accumulate over the views)."""
+    """Forward+backward ms/iter through torch.autograd (the loader's activations and the hand-written
+    backward behind autograd Functions).  One iteration = the 8 views rendered, compared with their
+    targets and back-propagated, gradients summed over the views: `ms_per_iter` with the 8 views in
+    one node (render_raw_views: one renderer per view, gradients added in place on the GPU),
+    `ms_per_iter_view_nodes` with one render_raw node and one backward call per view (autograd sums
+    the per-view gradient arrays)."""
     import numpy as np
     import torch
     from splatter_gb300 import BlendMode, Configuration, Renderer, camera, synthetic
-    from splatter_gb300.autograd import render_raw
+    from splatter_gb300.autograd import render_raw, render_raw_views
 
     n, W, H, views = 1_000_000, 1024, 1024, 8
     rec = synthetic.clustered(n, seed=args.seed + 11, sh_order=3)
@@ -577,17 +580,33 @@ def run_differentiation(args, iters=5, warmup=3):
             total = total + loss.detach()
         return total
 
-    for _ in range(warmup):
-        iteration()
-    torch.cuda.synchronize()
+    view_renderers = [r] + [Renderer(cfg) for _ in range(views - 1)]
+    target_stack = torch.stack(targets)
+
+    def iteration_views():
+        for t in leaves:
+            t.grad = None
+        imgs = render_raw_views(leaves[0], leaves[1], leaves[2], leaves[3], leaves[4], view_renderers, poses, W, H)
+        loss = ((imgs[..., :3] - target_stack) ** 2).sum()
+        loss.backward()
+        return loss.detach()
+
     stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(iters):
-        loss = iteration()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / iters
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(iters):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / iters, out
+
+    ms_nodes, loss_nodes = timed(iteration)
+    ms, loss = timed(iteration_views)
     # forward alone (no graph), same views
     with torch.no_grad():
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -600,6 +619,7 @@ def run_differentiation(args, iters=5, warmup=3):
     ms_fwd = f0.elapsed_time(f1) / iters
     finite = all(bool(torch.isfinite(t.grad).all()) for t in leaves)
     return {"workload": DIFF_WORKLOAD, "ms_per_iter": round(ms, 3), "ms_forward_per_iter": round(ms_fwd, 3),
+            "ms_per_iter_view_nodes": round(ms_nodes, 3), "loss_view_nodes": float(loss_nodes),
             "views": views, "splats": n, "iters": iters, "warmup": warmup, "loss": float(loss),
             "grads_finite": finite,
             "note": "device-timed (CUDA events around whole iterations, python/autograd overhead included)"}

@@ -225,6 +225,14 @@ SPL_API int spl_render_backward(spl_renderer* r, const spl_scene* scene, const f
                                 const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z,
                                 float* grad_rotation, float* grad_scale_alpha, float* grad_sh, void* stream);
 
+/* spl_render_backward, adding the frame's gradients into the arrays instead of storing them: the
+ * gradients of several frames (views) of one scene summed in place, frame after frame on one stream,
+ * with no per-frame gradient arrays to zero and add up.  Zero the arrays once before the first frame. */
+SPL_API int spl_render_backward_accumulate(spl_renderer* r, const spl_scene* scene, const float* image_device,
+                                           const float* grad_image_device, float* grad_x, float* grad_y,
+                                           float* grad_z, float* grad_rotation, float* grad_scale_alpha,
+                                           float* grad_sh, void* stream);
+
 /* The loader's activations (Scene::load_chunk, scene.rs:225-250) on device arrays of raw parameters,
  * for training: means (n x 3), quaternions (n x 4, scalar first), log-scales (n x 3) and opacity
  * logits (n) -> the arrays of a wrapped scene (x, y, z planes; unit rotations n x 4; scale + opacity

@@ -141,6 +141,7 @@ SIGNATURES = [
     ("spl_sort_pairs_no_alloc", I32, [P, P, P, P, U64, U32, P]),
     ("spl_scene_wrap", I32, [P, U64, P, P, P, P, P, P, ctypes.POINTER(P)]),
     ("spl_render_backward", I32, [P, P, P, P, P, P, P, P, P, P, P]),
+    ("spl_render_backward_accumulate", I32, [P, P, P, P, P, P, P, P, P, P, P]),
     ("spl_renderer_copy_record_gradients", I32, [P, P, U64, P]),
     ("spl_renderer_set_sort_mode", I32, [P, I32]),
     ("spl_frame_graph_create", I32, [P, U32, U32, U64, P, ctypes.POINTER(P)]),

@@ -7,8 +7,10 @@ file loader's activations first (Scene::load_chunk, scene.rs:225-250: rotor norm
 log-scales clamped to mean +- 5, sigmoid of the opacity logit) with the loader's own arithmetic on the
 GPU (spl_activate_splats) and chains its backward there too (spl_activate_splats_backward), so
 gradients reach the raw parameters a training loop optimises without torch elementwise kernels per
-frame.  `activate` is the same transform written in torch (a reference).  Depth order, culling and the 1/255 discard are constants of
-the frame (no gradient), as in any splat rasteriser.
+frame.  `render_raw_views` renders several views of the same raw parameters in one autograd node and
+sums their gradients in place on the GPU (spl_render_backward_accumulate).  `activate` is the same
+transform written in torch (a reference).  Depth order, culling and the 1/255 discard are constants
+of the frame (no gradient), as in any splat rasteriser.
 """
 import ctypes
 
@@ -18,7 +20,7 @@ from . import _lib
 from ._lib import check
 from .renderer import BlendMode, Renderer, _stream_ptr
 
-__all__ = ["render_splats", "render_raw", "activate", "activate_native"]
+__all__ = ["render_splats", "render_raw", "render_raw_views", "activate", "activate_native"]
 
 
 def _ptr(t):
@@ -103,14 +105,18 @@ class _RenderSplats:  # built lazily so that importing the package does not impo
         return cls.fn
 
 
+def _ensure_frame(r, scene, cam, w, h):
+    """Re-renders (scene, cam) on renderer r if r has rendered another frame since: the backward
+    reuses the renderer's frame state (sorted pairs, records, tile ranges)."""
+    key = (id(scene), cam.tobytes(), w, h)
+    if getattr(r, "_last_frame_key", None) != key:
+        r.render_frame(scene, cam, w, h)  # deterministic: the same frame again
+        r._last_frame_key = key
+
+
 def _frame_ready(ctx):
     """Re-renders the frame of this autograd node if the renderer has rendered another one since."""
-    r = ctx.renderer
-    w, h = ctx.size
-    key = (id(ctx.scene), ctx.cam.tobytes(), w, h)
-    if getattr(r, "_last_frame_key", None) != key:
-        r.render_frame(ctx.scene, ctx.cam, w, h)  # deterministic: the same frame again
-        r._last_frame_key = key
+    _ensure_frame(ctx.renderer, ctx.scene, ctx.cam, *ctx.size)
 
 
 class _RenderRaw:  # built lazily, like _RenderSplats
@@ -175,6 +181,77 @@ class _RenderRaw:  # built lazily, like _RenderSplats
         return cls.fn
 
 
+class _RenderRawViews:  # built lazily, like _RenderSplats
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is None:
+            torch = _import_torch()
+
+            class RenderRawViews(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, means, quats, log_scales, logits, sh, renderers, cameras, width, height):
+                    means, quats, log_scales, logits, sh = (t.contiguous() for t in (means, quats, log_scales, logits,
+                                                                                      sh))
+                    n = quats.shape[0]
+                    f32 = dict(device=quats.device, dtype=torch.float32)
+                    xyz = torch.empty((3, n), **f32)
+                    rot = torch.empty((n, 4), **f32)
+                    sa = torch.empty((n, 4), **f32)
+                    lib = _lib.load()
+                    check(lib.spl_activate_splats(n, _ptr(means), _ptr(quats), _ptr(log_scales), _ptr(logits),
+                                                  _ptr(xyz[0]), _ptr(xyz[1]), _ptr(xyz[2]), _ptr(rot), _ptr(sa),
+                                                  _stream_ptr(None)))
+                    out = torch.empty((len(cameras), height, width, 4), **f32)
+                    scenes, views = {}, []
+                    for v, cam in enumerate(cameras):
+                        r = renderers[v % len(renderers)]
+                        if id(r) not in scenes:
+                            scenes[id(r)] = _WrappedScene(r, xyz, rot, sa, sh)
+                        scene = scenes[id(r)]
+                        c = np.ascontiguousarray(np.asarray(cam, np.float32).reshape(16))
+                        r.render_frame(scene, c, width, height, out=out[v])
+                        r._last_frame_key = (id(scene), c.tobytes(), width, height)
+                        views.append((r, scene, c))
+                    ctx.views = views
+                    ctx.size = (width, height)
+                    ctx.save_for_backward(out, quats, log_scales)
+                    return out
+
+                @staticmethod
+                def backward(ctx, grad_out):
+                    out, quats, log_scales = ctx.saved_tensors
+                    w, h = ctx.size
+                    xyz, rot, sa, sh = ctx.views[0][1]._keep
+                    n = rot.shape[0]
+                    gxyz = torch.zeros_like(xyz)
+                    grot = torch.zeros_like(rot)
+                    gsa = torch.zeros_like(sa)
+                    gsh = torch.zeros_like(sh)
+                    g = grad_out.contiguous().float()
+                    st = _stream_ptr(None)
+                    # the views in order, each adding its gradients in place
+                    for v, (r, scene, c) in enumerate(ctx.views):
+                        _ensure_frame(r, scene, c, w, h)
+                        check(r._lib.spl_render_backward_accumulate(r.handle, scene.handle, _ptr(out[v]), _ptr(g[v]),
+                                                                    _ptr(gxyz[0]), _ptr(gxyz[1]), _ptr(gxyz[2]),
+                                                                    _ptr(grot), _ptr(gsa), _ptr(gsh), st))
+                    g_means = torch.empty((n, 3), device=rot.device, dtype=torch.float32)
+                    g_quats = torch.empty((n, 4), device=rot.device, dtype=torch.float32)
+                    g_logs = torch.empty((n, 3), device=rot.device, dtype=torch.float32)
+                    g_logits = torch.empty((n,), device=rot.device, dtype=torch.float32)
+                    check(_lib.load().spl_activate_splats_backward(n, _ptr(quats), _ptr(log_scales), _ptr(rot),
+                                                                   _ptr(sa), _ptr(gxyz[0]), _ptr(gxyz[1]),
+                                                                   _ptr(gxyz[2]), _ptr(grot), _ptr(gsa),
+                                                                   _ptr(g_means), _ptr(g_quats), _ptr(g_logs),
+                                                                   _ptr(g_logits), st))
+                    return g_means, g_quats, g_logs, g_logits, gsh, None, None, None, None
+
+            cls.fn = RenderRawViews
+        return cls.fn
+
+
 def render_splats(xyz, rotation, scale_alpha, sh, renderer: Renderer, camera_to_world, width, height):
     """Differentiable frame.  xyz: (3, N) centre planes; rotation: (N, 4) scalar first; scale_alpha:
     (N, 4) scale xyz + opacity; sh: (N, 48).  Returns (H, W, 4) float32 (r, g, b, T)."""
@@ -220,3 +297,28 @@ def render_raw(means, quats, log_scales, opacity_logits, sh, renderer, camera_to
             raise ValueError("render_raw: float32 CUDA tensors (N, 3), (N, 4), (N, 3), (N,), (N, 48) expected")
     return _RenderRaw.get().apply(means, quats, log_scales, opacity_logits, sh, renderer, camera_to_world, width,
                                   height)
+
+
+def render_raw_views(means, quats, log_scales, opacity_logits, sh, renderers, cameras, width, height):
+    """render_raw over several views of the same parameters in one autograd node: returns
+    (len(cameras), H, W, 4) float32.  The backward adds every view's gradients into one set of arrays
+    in place (spl_render_backward_accumulate), view after view, and chains the loader's activations
+    once, instead of a gradient array per view that autograd zeroes and sums.  `renderers`: one
+    Renderer, or a sequence used round robin over the views; a renderer keeps the frame state of the
+    last view it rendered, so with fewer renderers than views the backward renders the other views
+    again (same frames).  Gradients equal the per-view render_raw gradients summed over the views, to
+    rounding: the raster backward sums with float atomics, and the activations' chain rule is
+    applied to the sum instead of to each view."""
+    if isinstance(renderers, Renderer):
+        renderers = [renderers]
+    renderers = list(renderers)
+    cameras = list(cameras)
+    if not renderers or not cameras:
+        raise ValueError("render_raw_views: at least one renderer and one camera")
+    if any(r.config.blend_mode != BlendMode.FP32 for r in renderers):
+        raise ValueError("render_raw_views needs renderers with blend_mode FP32")
+    for t, shape in ((means, 3), (quats, 4), (log_scales, 3), (sh, 48)):
+        if t.dim() != 2 or t.shape[1] != shape or t.dtype.itemsize != 4 or not t.is_cuda:
+            raise ValueError("render_raw_views: float32 CUDA tensors (N, 3), (N, 4), (N, 3), (N,), (N, 48) expected")
+    return _RenderRawViews.get().apply(means, quats, log_scales, opacity_logits, sh, renderers, cameras, width,
+                                       height)

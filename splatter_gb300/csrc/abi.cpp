@@ -477,9 +477,9 @@ int spl_renderer_launches_per_frame(const spl_renderer* r, uint32_t width, uint3
     return 1 + 1 + 1 + depth_sort + 1 + 1 + (coop ? 1 : pair_passes) + 1 + (r->order_tiles ? 1 : 0) + 1;
 }
 
-int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
-                        const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z, float* grad_rotation,
-                        float* grad_scale_alpha, float* grad_sh, void* stream) {
+static int render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
+                           const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z,
+                           float* grad_rotation, float* grad_scale_alpha, float* grad_sh, void* stream, bool accumulate) {
     if (!r || !scene || !image_device || !grad_image_device || !grad_x || !grad_y || !grad_z || !grad_rotation ||
         !grad_scale_alpha || !grad_sh)
         return fail(SPL_ERR_INVALID, "NULL argument");
@@ -497,9 +497,23 @@ int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* im
                     r->order_tiles ? r->tile_order : nullptr, r->final_pair_vals, r->rec, reinterpret_cast<const float4*>(image_device),
                     reinterpret_cast<const float4*>(grad_image_device), r->grad_rec, (uint32_t)scene->n, grad_x,
                     grad_y, grad_z, reinterpret_cast<float4*>(grad_rotation), reinterpret_cast<float4*>(grad_scale_alpha),
-                    grad_sh, st);
+                    grad_sh, accumulate, st);
     CU(cudaGetLastError());
     return SPL_OK;
+}
+
+int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
+                        const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z, float* grad_rotation,
+                        float* grad_scale_alpha, float* grad_sh, void* stream) {
+    return render_backward(r, scene, image_device, grad_image_device, grad_x, grad_y, grad_z, grad_rotation,
+                           grad_scale_alpha, grad_sh, stream, false);
+}
+
+int spl_render_backward_accumulate(spl_renderer* r, const spl_scene* scene, const float* image_device,
+                                   const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z,
+                                   float* grad_rotation, float* grad_scale_alpha, float* grad_sh, void* stream) {
+    return render_backward(r, scene, image_device, grad_image_device, grad_x, grad_y, grad_z, grad_rotation,
+                           grad_scale_alpha, grad_sh, stream, true);
 }
 
 int spl_renderer_copy_record_gradients(spl_renderer* r, float* dst_device, uint64_t capacity, void* stream) {

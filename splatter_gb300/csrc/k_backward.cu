@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
                                                              const uint2* __restrict__ boxes,
                                                              const float* __restrict__ grad_rec, float* gx, float* gy,
                                                              float* gz, float4* grot, float4* gscale_alpha,
-                                                             float* gsh) {
+                                                             float* gsh, bool accumulate) {
     const uint32_t V = fc->visible;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < V; slot += gridDim.x * blockDim.x) {
         const float* gr = grad_rec + (size_t)slot * GR;
@@ -266,11 +266,20 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
             acc += (g[4] * o.A11.d + g[5] * o.B1r.d);
             gin[dir] = isfinite(acc) ? acc : 0.0f;
         }
-        gx[i] = gin[0];
-        gy[i] = gin[1];
-        gz[i] = gin[2];
-        grot[i] = make_float4(gin[3], gin[4], gin[5], gin[6]);
-        gscale_alpha[i] = make_float4(gin[7], gin[8], gin[9], g[6]);
+        if (accumulate) {  // several frames' gradients summed in place, one frame after another
+            const float4 r0 = grot[i], s0 = gscale_alpha[i];
+            gx[i] += gin[0];
+            gy[i] += gin[1];
+            gz[i] += gin[2];
+            grot[i] = make_float4(r0.x + gin[3], r0.y + gin[4], r0.z + gin[5], r0.w + gin[6]);
+            gscale_alpha[i] = make_float4(s0.x + gin[7], s0.y + gin[8], s0.z + gin[9], s0.w + g[6]);
+        } else {
+            gx[i] = gin[0];
+            gy[i] = gin[1];
+            gz[i] = gin[2];
+            grot[i] = make_float4(gin[3], gin[4], gin[5], gin[6]);
+            gscale_alpha[i] = make_float4(gin[7], gin[8], gin[9], g[6]);
+        }
         // SH: rgb_c = 0.5 + sum_k B_k(d) sh[3k + c]
         const float vx = cx - u.camera[12], vy = cy - u.camera[13], vz = cz - u.camera[14];
         const float len = sqrtf((vx * vx + vy * vy) + vz * vz);
@@ -278,11 +287,20 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
         sh_basis<SHO>(vx / len, vy / len, vz / len, B);
         float* o = gsh + (size_t)i * 48;
         constexpr int NK = (SHO + 1) * (SHO + 1);
+        if (accumulate) {
 #pragma unroll
-        for (int k = 0; k < NK; ++k) {
-            o[3 * k + 0] = B[k] * g[7];
-            o[3 * k + 1] = B[k] * g[8];
-            o[3 * k + 2] = B[k] * g[9];
+            for (int k = 0; k < NK; ++k) {
+                o[3 * k + 0] += B[k] * g[7];
+                o[3 * k + 1] += B[k] * g[8];
+                o[3 * k + 2] += B[k] * g[9];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NK; ++k) {
+                o[3 * k + 0] = B[k] * g[7];
+                o[3 * k + 1] = B[k] * g[8];
+                o[3 * k + 2] = B[k] * g[9];
+            }
         }
     }
 }
@@ -292,7 +310,7 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
                      const uint32_t* tile_order, const uint32_t* pair_vals, const float4* rec, const float4* image,
                      const float4* grad_image, float* grad_rec,
                      uint32_t max_n, float* gx, float* gy, float* gz, float4* grot, float4* gscale_alpha, float* gsh,
-                     cudaStream_t st) {
+                     bool accumulate, cudaStream_t st) {
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];
     const int tiles_x = (W + TILE_PIXELS - 1) / TILE_PIXELS, tiles_y = (H + TILE_PIXELS - 1) / TILE_PIXELS;
     const float psx = (2.0f * u.view_size[0]) / (float)W;
@@ -315,7 +333,7 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
     if (blocks > 152u * 16u) blocks = 152u * 16u;
 #define PB(SHO, COV)                                                                                        \
     k_preprocess_backward<SHO, COV><<<blocks, 128, 0, st>>>(s, u, idx, fc, boxes, grad_rec, gx, gy, gz, grot,       \
-                                                            gscale_alpha, gsh)
+                                                            gscale_alpha, gsh, accumulate)
     switch (sh_order * 2 + (covariance ? 1 : 0)) {
         case 0: PB(0, false); break;
         case 1: PB(0, true); break;

@@ -127,7 +127,7 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
                      const float4* grad_image,
                      float* grad_rec,
                      uint32_t max_n, float* gx, float* gy, float* gz, float4* grot, float4* gscale_alpha, float* gsh,
-                     cudaStream_t st);
+                     bool accumulate, cudaStream_t st);
 void launch_histogram(const uint32_t* keys, const uint32_t* n_ptr, uint32_t n_cap, uint32_t* hist4x256,
                       cudaStream_t st);
 void launch_set_count(uint32_t* dst, uint32_t value, cudaStream_t st);

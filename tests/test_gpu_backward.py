@@ -291,6 +291,37 @@ def test_raw_parameter_gradients_through_autograd(cuda):
         assert close(got, want)
 
 
+def test_render_raw_views_equals_per_view_sum(cuda):
+    """render_raw_views: the stacked frames equal render_raw's frame of each view bit for bit, and
+    the in-place accumulated gradients equal the per-view render_raw gradients that autograd sums
+    over the views (to the rounding of the float atomics and of the activations' chain rule applied
+    to the sum).  Two renderers for three views, so the backward renders one view again."""
+    import torch
+    from splatter_gb300.autograd import render_raw_views
+    n, W, H = 5000, 128, 96
+    rec, cam, cfg = _setup(n, W, H, seed=61, scale_boost=0.5)
+    cams = [cam] + [camera.look_at(np.array([math.sin(a) * 7.0, 0.8, math.cos(a) * 7.0], np.float32),
+                                   np.zeros(3, np.float32)) for a in (0.4, -0.7)]
+    rs = [Renderer(cfg), Renderer(cfg)]
+
+    def leaves():
+        return [torch.tensor(rec[:, a:b], device="cuda").squeeze(1).contiguous().requires_grad_(True)
+                for a, b in ((0, 3), (58, 62), (55, 58), (54, 55), (6, 54))]
+    weights = torch.rand((len(cams), H, W, 3), device="cuda", generator=torch.Generator("cuda").manual_seed(5))
+    batched = leaves()
+    imgs = render_raw_views(*batched, rs, cams, W, H)
+    (imgs[..., :3] ** 2 * weights).sum().backward()
+    single = leaves()
+    for v, c in enumerate(cams):
+        img = render_raw(*single, rs[0], c, W, H)
+        assert torch.equal(img, imgs[v])
+        (img[..., :3] ** 2 * weights[v]).sum().backward()
+    torch.cuda.synchronize()
+    for got, want in zip((t.grad for t in batched), (t.grad for t in single)):
+        assert float(want.abs().max()) > 0.0
+        assert torch.allclose(got, want, rtol=1e-4, atol=1e-4 * float(want.abs().max()))
+
+
 def test_backward_requires_fp32_blend(cuda):
     import torch
     from splatter_gb300 import SplatterError

@@ -233,14 +233,14 @@ def load_peaks():
 
 
 # DRAM traffic per unit of the dominant kernel, from one ncu capture of a smaller case of the same
-# workload (profiles/k_raster_3m_1080p.md: 3M splats, 1920x1080, 3,353,969 pairs, 242.7 MB read + 7.2
+# workload (profiles/k_raster_3m_1080p.md: 3M splats, 1920x1080, 3,353,969 pairs, 240.6 MB read + 6.4
 # MB written): the reads grow with the pairs, the image write is per launch.  The bench scales it to
 # its own frames by their pair counts.
-TRAFFIC_PER_UNIT = {"raster": {"per_pair": 242.7e6 / 3353969.0, "per_launch": 7.2e6,
+TRAFFIC_PER_UNIT = {"raster": {"per_pair": 240.6e6 / 3353969.0, "per_launch": 6.4e6,
                                "source": "profiles/k_raster_3m_1080p.md (3M-splat capture, scaled by pairs)"}}
 # The raster is bound by instruction issue, not HBM: the fraction of issue slots its warps used in the
 # same capture (smsp__issue_active, pct of peak, active), reported beside the HBM figure.
-ISSUE_ACTIVE = {"raster": {"frac": 0.855, "source": "profiles/k_raster_3m_1080p.md smsp__issue_active"}}
+ISSUE_ACTIVE = {"raster": {"frac": 0.836, "source": "profiles/k_raster_3m_1080p.md smsp__issue_active"}}
 
 
 def stage_traffic(stage, P):

@@ -558,9 +558,13 @@ const float FP32_T_MIN = 1e-4f;
 const float ALPHA_MIN = 1.0f / 255.0f;
 
 // Rasterise the ordered draw list into one 16x16 tile (fragment + blend, shaders.wgsl:580-592,
-// renderer.rs:260-271; clear renderer.rs:441-442).
+// renderer.rs:260-271; clear renderer.rs:441-442).  With COUNT the tile is not written; work[0..2]
+// gain the tile's (pixel, record) pairs with the pixel inside the record's pixel box, those whose
+// pixel centre also passes the coverage test (every pair, also after the pixel has finished), and
+// the blend steps the pixel performs (coverage, alpha >= 1/255, before it finishes).
+template <bool COUNT>
 void raster_tile(const OU& u, const OCfg& cfg, const float* recs, const uint32_t* list, size_t nlist, int tx, int ty,
-                 void* out) {
+                 void* out, uint64_t* work = nullptr) {
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];
     const float m = u.margin;
     for (int py = ty * 16; py < std::min(H, ty * 16 + 16); ++py) {
@@ -568,11 +572,13 @@ void raster_tile(const OU& u, const OCfg& cfg, const float* recs, const uint32_t
             const float X = (float)px + 0.5f, Y = (float)py + 0.5f;
             int cr = 0, cg = 0, cb = 0, ta = 255;
             float fr = 0.f, fg = 0.f, fb = 0.f, ft = 1.f;
+            bool finished = false;
             for (size_t li = 0; li < nlist; ++li) {
                 const float* rc = recs + (size_t)list[li] * 16;
                 const uint32_t lo = float_to_bits(rc[7]), hi = float_to_bits(rc[11]);
                 const int x0 = (int)(lo & 0xFFFFu), y0 = (int)(lo >> 16), x1 = (int)(hi & 0xFFFFu), y1 = (int)(hi >> 16);
                 if (px < x0 || px > x1 || py < y0 || py > y1) continue;
+                if (COUNT) ++work[0];
                 const float tcx = std::fmaf(rc[1], Y, std::fmaf(rc[0], X, rc[2]));
                 const float tcy = std::fmaf(rc[4], Y, std::fmaf(rc[3], X, rc[5]));
                 if (cfg.use_unaligned_rectangles) {
@@ -583,9 +589,14 @@ void raster_tile(const OU& u, const OCfg& cfg, const float* recs, const uint32_t
                     const float dx = std::fmaf(sx, X, rc[12]), dy = std::fmaf(sy, Y, rc[13]);
                     if (!(std::fabs(dx) <= rc[14] && std::fabs(dy) <= rc[14])) continue;
                 }
+                if (COUNT) {
+                    ++work[1];
+                    if (finished) continue;
+                }
                 const float power = std::fmaf(tcx, tcx, tcy * tcy);
                 const float alpha = rc[6] * o_expf(-0.5f * power);
                 if (alpha < ALPHA_MIN) continue;
+                if (COUNT) ++work[2];
                 const float sr = clamp01(rc[8] * alpha), sg = clamp01(rc[9] * alpha), sb = clamp01(rc[10] * alpha);
                 const float sa = clamp01(alpha);
                 if (cfg.blend_mode == 0) {
@@ -594,15 +605,17 @@ void raster_tile(const OU& u, const OCfg& cfg, const float* recs, const uint32_t
                     cg = (int)rintf(clamp01(sg * dA + g_lut[cg]) * 255.0f);
                     cb = (int)rintf(clamp01(sb * dA + g_lut[cb]) * 255.0f);
                     ta = (int)rintf(clamp01(dA * (1.0f - sa)) * 255.0f);
-                    if (ta == 0) break;
+                    finished = ta == 0;
                 } else {
                     fr = sr * ft + fr;
                     fg = sg * ft + fg;
                     fb = sb * ft + fb;
                     ft = ft * (1.0f - sa);
-                    if (ft < FP32_T_MIN) break;
+                    finished = ft < FP32_T_MIN;
                 }
+                if (!COUNT && finished) break;
             }
+            if (COUNT) continue;
             const size_t pix = (size_t)py * W + px;
             if (cfg.blend_mode == 0) {
                 uint8_t* o = (uint8_t*)out + pix * 4;
@@ -759,14 +772,22 @@ OAPI uint64_t oracle_preprocess_f64(const void* uni, const void* cfg, const floa
 }
 
 // Rasterise records (16 floats each, in draw order) into out (RGBA8 for unorm8, float4 for fp32).
-// tile_stride > 1 renders only every tile_stride-th 16x16 tile (a bounded sample for timing).
+// tile_stride > 1 renders only every tile_stride-th 16x16 tile (a bounded sample for timing).  With
+// work != nullptr nothing is rendered and work[0..2] receive raster_tile<true>'s counts.
 static void raster_impl(const void* uni, const void* cfgp, const float* recs, uint64_t n, void* out, int threads,
-                        int tile_stride);
+                        int tile_stride, uint64_t* work = nullptr);
 OAPI void oracle_raster(const void* uni, const void* cfgp, const float* recs, uint64_t n, void* out, int threads) {
     raster_impl(uni, cfgp, recs, n, out, threads, 1);
 }
+// The raster's work for a frame's records: work[0] (pixel, record) pairs inside the records' pixel
+// boxes, work[1] of those whose pixel centre passes the coverage test, work[2] blend steps performed.
+OAPI void oracle_raster_work(const void* uni, const void* cfgp, const float* recs, uint64_t n, int threads,
+                             uint64_t* work) {
+    work[0] = work[1] = work[2] = 0;
+    raster_impl(uni, cfgp, recs, n, nullptr, threads, 1, work);
+}
 static void raster_impl(const void* uni, const void* cfgp, const float* recs, uint64_t n, void* out, int threads,
-                        int tile_stride) {
+                        int tile_stride, uint64_t* work) {
     const OU& u = *(const OU*)uni;
     const OCfg& cfg = *(const OCfg*)cfgp;
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];
@@ -781,12 +802,19 @@ static void raster_impl(const void* uni, const void* cfgp, const float* recs, ui
             for (int tx = x0 / 16; tx <= x1 / 16; ++tx) lists[(size_t)ty * TX + tx].push_back((uint32_t)i);
     }
     std::atomic<int64_t> next{0};
+    std::atomic<uint64_t> total[3] = {{0}, {0}, {0}};
     auto worker = [&] {
+        uint64_t mine[3] = {0, 0, 0};
         for (;;) {
             const int64_t t = next.fetch_add(1) * (int64_t)tile_stride;
             if (t >= (int64_t)TX * TY) break;
-            raster_tile(u, cfg, recs, lists[t].data(), lists[t].size(), (int)(t % TX), (int)(t / TX), out);
+            if (work)
+                raster_tile<true>(u, cfg, recs, lists[t].data(), lists[t].size(), (int)(t % TX), (int)(t / TX), out,
+                                  mine);
+            else
+                raster_tile<false>(u, cfg, recs, lists[t].data(), lists[t].size(), (int)(t % TX), (int)(t / TX), out);
         }
+        for (int k = 0; k < 3; ++k) total[k] += mine[k];
     };
     if (threads <= 1) {
         worker();
@@ -795,6 +823,8 @@ static void raster_impl(const void* uni, const void* cfgp, const float* recs, ui
         for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
         for (auto& th : pool) th.join();
     }
+    if (work)
+        for (int k = 0; k < 3; ++k) work[k] = total[k];
 }
 
 OAPI uint64_t oracle_cpu_sort_fallback(const void* uni, const float* positions, uint64_t n, uint32_t* entries);

@@ -12,7 +12,7 @@ import numpy as np
 from . import build_oracle
 
 __all__ = [
-    "lib", "uniforms", "cull_keys", "draw_list", "preprocess", "raster", "render", "load_transform",
+    "lib", "uniforms", "cull_keys", "draw_list", "preprocess", "raster", "raster_work", "render", "load_transform",
     "cpu_sort_fallback", "cpu_frame_timed", "expf", "GradContext", "OCFG", "UNIFORM_DTYPE", "config_struct",
 ]
 
@@ -41,6 +41,8 @@ def lib():
             f.argtypes = [P, P, P, P, P, P, P, P, u64, P, P, ctypes.c_int]
         L.oracle_raster.restype = None
         L.oracle_raster.argtypes = [P, P, P, u64, P, ctypes.c_int]
+        L.oracle_raster_work.restype = None
+        L.oracle_raster_work.argtypes = [P, P, P, u64, ctypes.c_int, P]
         L.oracle_render.restype = u64
         L.oracle_render.argtypes = [P, P, P, P, P, P, P, u64, P, ctypes.c_int, P]
         L.oracle_load_transform.restype = None
@@ -145,6 +147,18 @@ def raster(u, cfg, records, threads=8):
         out = np.zeros((H, W, 4), np.float32)
     lib().oracle_raster(_p(u), _p(cfg), _p(recs), recs.shape[0], _p(out), int(threads))
     return out
+
+
+def raster_work(u, cfg, records, threads=8):
+    """The raster's work for a frame's records in draw order (not a reference function; the
+    algorithmic unit of the raster's compute roofline): `box` (pixel, record) pairs with the pixel
+    inside the record's pixel box, `covered` those whose pixel centre passes the coverage test of
+    shaders.wgsl:580-583 (all of them, also after the pixel has finished), `blended` the blend steps
+    the pixels perform (coverage, alpha >= 1/255, before the pixel finishes)."""
+    recs = _c(records, np.float32).reshape(-1, 16)
+    work = np.zeros(3, np.uint64)
+    lib().oracle_raster_work(_p(u), _p(cfg), _p(recs), recs.shape[0], int(threads), _p(work))
+    return {"box": int(work[0]), "covered": int(work[1]), "blended": int(work[2])}
 
 
 def render(u, cfg, scene, threads=8):

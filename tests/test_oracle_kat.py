@@ -225,3 +225,55 @@ def test_dev_scene_golden():
         import hashlib
         assert hashlib.sha256(img.tobytes()).hexdigest() == case["sha256"], case["name"]
         assert list(st) == case["stats"]
+
+
+@pytest.mark.parametrize("blend", [0, 1])
+def test_raster_work_counts(blend):
+    """oracle.raster_work (the raster's algorithmic unit) against a per-record sweep over all pixels
+    in numpy: pairs inside the pixel boxes, pairs passing the coverage test, and blend steps before
+    each pixel finishes (T == 0 in unorm8, T < 1e-4 in fp32)."""
+    W, H = 72, 40
+    rec = synthetic.plain_small(400, seed=9, sh_order=0)
+    rec[:, 55:58] += 1.5  # splats a few pixels wide
+    sc = oracle.load_transform(rec)
+    cam = camera.look_at([0.4, 0.3, -9.0], [0.0, 0.0, 0.0])
+    u = oracle.uniforms(cam, W, H, fovy=math.radians(60))
+    cfg = oracle.config_struct(sh_order=0, blend_mode=blend)
+    _, idx, _, nd = oracle.draw_list(u, 2, sc["center"])
+    recs, _, _ = oracle.preprocess(u, cfg, sc, idx[:nd], threads=2)
+    work = oracle.raster_work(u, cfg, recs, threads=3)
+    f32, m = np.float32, np.float32(u["margin"][0])
+    X = np.arange(W, dtype=f32)[None, :] + f32(0.5)
+    Y = np.arange(H, dtype=f32)[:, None] + f32(0.5)
+    px, py = np.arange(W)[None, :], np.arange(H)[:, None]
+    fma = lambda a, b, c: (np.float64(a) * np.float64(b) + np.float64(c)).astype(f32)
+    box = cov = blended = 0
+    ta = np.full((H, W), 255, np.int64)
+    ft = np.ones((H, W), f32)
+    done = np.zeros((H, W), bool)
+    lut = np.arange(256, dtype=f32) / f32(255.0)
+    for rc in recs.astype(f32):
+        lo, hi = int(rc[7:8].view(np.uint32)[0]), int(rc[11:12].view(np.uint32)[0])
+        x0, y0, x1, y1 = lo & 0xFFFF, lo >> 16, hi & 0xFFFF, hi >> 16
+        inb = (px >= x0) & (px <= x1) & (py >= y0) & (py <= y1)
+        tcx = fma(rc[1], Y, fma(rc[0], X, rc[2]))
+        tcy = fma(rc[4], Y, fma(rc[3], X, rc[5]))
+        c = inb & (np.abs(tcx) <= m) & (np.abs(tcy) <= m)
+        box += int(inb.sum())
+        cov += int(c.sum())
+        live = c & ~done
+        for yy, xx in zip(*np.nonzero(live)):
+            power = fma(tcx[yy, xx], tcx[yy, xx], tcy[yy, xx] * tcy[yy, xx])
+            alpha = f32(rc[6] * f32(oracle.expf(f32(-0.5) * power)))
+            if alpha < f32(1.0) / f32(255.0):
+                continue
+            blended += 1
+            sa = np.clip(alpha, f32(0.0), f32(1.0))
+            if blend == 0:
+                ta[yy, xx] = int(np.rint(np.clip(lut[ta[yy, xx]] * (f32(1.0) - sa), 0, 1) * f32(255.0)))
+                done[yy, xx] = ta[yy, xx] == 0
+            else:
+                ft[yy, xx] = ft[yy, xx] * (f32(1.0) - sa)
+                done[yy, xx] = ft[yy, xx] < f32(1e-4)
+    assert box > cov > blended > 0
+    assert work == {"box": box, "covered": cov, "blended": blended}

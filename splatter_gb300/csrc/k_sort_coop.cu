@@ -11,7 +11,7 @@
 //   3. offsets: each CTA reads its column of prefixes and the 256 totals (global digit bases)
 //   4. scatter, sub-tile by sub-tile (4096 keys): warp-level multisplit ranking (digit match by eight
 //      ballots),
-//      per-digit warp prefixes, keys then values staged through shared memory and written as runs
+//      per-digit warp prefixes, keys and values staged together through shared memory and written as runs
 //   5. bounded grid barrier (the next pass reads this pass's output)
 // The ranking keeps equal digits in input order, so every pass is stable, like the onesweep passes.
 // Every barrier wait is bounded: on timeout the error bit is raised and the kernel runs to its end
@@ -29,7 +29,8 @@ constexpr int CS_TILE = CS_THREADS * CS_KPT;  // 4096 keys per sub-tile
 static_assert(CS_THREADS % 256 == 0, "the per-digit phases map 256 digits onto groups of threads");
 
 struct CoopSmem {
-    uint32_t buf[CS_TILE];             // staging for keys, then values
+    uint32_t buf[CS_TILE];             // keys of the sub-tile in digit order
+    uint32_t vbuf[CS_TILE];            // their values
     uint32_t wcnt[CS_WARPS][256];      // per-warp digit counts -> exclusive prefixes
     uint32_t part[CS_NQ][256];         // partial sums over groups of warps / of the count table
     uint32_t base[256];                // global output base of each digit for this CTA
@@ -278,41 +279,29 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
                 const uint32_t e = wb + 32u * j;
                 if (e < tb + tn) {
                     const uint32_t d = (key[j] >> shift) & 255u;
-                    pos[j] += sm.dstart[d] + sm.wcnt[w][d];
-                    sm.buf[pos[j]] = key[j];
+                    const uint32_t p = pos[j] + sm.dstart[d] + sm.wcnt[w][d];
+                    sm.buf[p] = key[j];
+                    sm.vbuf[p] = val[j];
                 }
             }
             __syncthreads();
-            uint32_t dig[CS_KPT];
+            // keys and values leave together: each digit's run is consecutive in the output
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
                 const uint32_t i = tid + CS_THREADS * j;
-                dig[j] = 0u;
                 if (i < tn) {
                     const uint32_t k = sm.buf[i];
-                    dig[j] = (k >> shift) & 255u;
-                    const uint32_t g = sm.base[dig[j]] + sm.running[dig[j]] + (i - sm.dstart[dig[j]]);
-                    if (g < n) kout[g] = k;
+                    const uint32_t d = (k >> shift) & 255u;
+                    const uint32_t g = sm.base[d] + sm.running[d] + (i - sm.dstart[d]);
+                    if (g < n) {
+                        kout[g] = k;
+                        vout[g] = sm.vbuf[i];
+                    }
                 }
             }
             __syncthreads();
-#pragma unroll
-            for (int j = 0; j < CS_KPT; ++j) {
-                const uint32_t e = wb + 32u * j;
-                if (e < tb + tn) sm.buf[pos[j]] = val[j];
-            }
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < CS_KPT; ++j) {
-                const uint32_t i = tid + CS_THREADS * j;
-                if (i < tn) {
-                    const uint32_t g = sm.base[dig[j]] + sm.running[dig[j]] + (i - sm.dstart[dig[j]]);
-                    if (g < n) vout[g] = sm.buf[i];
-                }
-            }
-            __syncthreads();
+            // read by the next sub-tile's writes only, after its barriers
             if (tid < 256) sm.running[tid] += sm.tcount[tid];
-            __syncthreads();
         }
         // ---- 5. the next pass reads this pass's output ----
         grid_barrier(bar, G, spin_limit, err);

@@ -7,6 +7,8 @@
 #include <mutex>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX v3: no-op calls unless a profiler is attached
+
 #include "../../include/splatter.h"
 #include "spl_types.h"
 
@@ -103,6 +105,7 @@ struct spl_renderer {
     // stage profiling: events 0..7 on the frame's stream
     bool profiling = false;
     cudaEvent_t ev_prof[8] = {};
+    nvtxRangeId_t nvtx_stage = 0;  // the open stage range of the frame being enqueued
 
 
     void release() {
@@ -120,8 +123,15 @@ struct spl_renderer {
     }
     uint64_t sort_tiles() const { return (max_n + SORT_TILE - 1) / SORT_TILE; }
     uint64_t pair_tiles() const { return (pair_cap + SORT_TILE - 1) / SORT_TILE; }
+    // Stage boundary i of a frame (0: before the cull ... 7: after the raster): a CUDA event when
+    // profiling, and an NVTX range per stage around its launches, so that a system profiler shows
+    // the stages on the host timeline and their kernels under them.
     void mark(int i, cudaStream_t s) {
+        static const char* const stage[7] = {"spl cull", "spl vertex", "spl depth sort", "spl binning",
+                                             "spl pair sort", "spl tile ranges", "spl raster"};
         if (profiling) cudaEventRecord(ev_prof[i], s);
+        if (i > 0 && nvtx_stage) nvtxRangeEnd(nvtx_stage);
+        nvtx_stage = i < 7 ? nvtxRangeStartA(stage[i]) : 0;
     }
 };
 

@@ -1,11 +1,12 @@
 """The C ABI from a compiled caller: tests/abi_consumer.c, built against include/splatter.h and
 libsplatter_cuda.so alone (no Python between them), the way the reference's Rust crate would bind it.
 
-Without a GPU: the header compiles as strict C11 and as C++17, the program links, and the host-only
-entry points behave.  With a GPU: the program renders the reference's dev-test scene
+Without a GPU: the header compiles as strict C11 and as C++17, its structs have the layouts the
+ctypes mirror declares, the program links, and the host-only entry points behave.  With a GPU: the program renders the reference's dev-test scene
 (Scene::new_dev_test, scene.rs:158-192) and its images equal the committed golden images of the
 oracle (tests/golden/dev_scene.json) byte for byte, with the same visible and drawn counts.
 """
+import ctypes
 import hashlib
 import json
 import os
@@ -85,3 +86,35 @@ def test_dev_scene_rendered_from_c_matches_golden(tmp_path):
         img = open(out, "rb").read()
         assert len(img) == case["width"] * case["height"] * 4
         assert hashlib.sha256(img).hexdigest() == case["sha256"], case["name"]
+
+
+def test_struct_layouts_match_the_ctypes_mirror(tmp_path):
+    """Every struct of the header has the size and field offsets that splatter_gb300/_lib.py declares
+    for ctypes (a mismatch would pass wrong values silently through the ABI)."""
+    from splatter_gb300 import _lib
+    structs = {"spl_config": _lib.SplConfig, "spl_frame_info": _lib.SplFrameInfo,
+               "spl_server_config": _lib.SplServerConfig, "spl_request": _lib.SplRequest,
+               "spl_completion": _lib.SplCompletion, "spl_server_stats": _lib.SplServerStats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "splatter.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'    printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    r = subprocess.run([_cc(), *STRICT, "-I", os.path.join(ROOT, "include"), str(src), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    seen = 0
+    for line in out:
+        if not line:
+            continue
+        cname, what, value = line.split()
+        py = structs[cname]
+        want = ctypes.sizeof(py) if what == "size" else getattr(py, what).offset
+        assert int(value) == want, (cname, what, int(value), want)
+        seen += 1
+    assert seen == len(structs) + sum(len(py._fields_) for py in structs.values())

@@ -106,3 +106,15 @@ def test_depth_sorting_enum_matches_header():
     text = open(os.path.join(ROOT, "include", "splatter.h")).read()
     for m in DepthSorting:
         assert re.search(rf"#define SPL_DEPTH_SORTING_{m.name} {int(m)}\b", text), m
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without the built library the package raises; there is no CPU fallback to route to."""
+    import subprocess
+    import sys
+    code = ("import splatter_gb300._lib as L\n"
+            f"L.LIB_PATH = {str(tmp_path / 'absent.so')!r}\n"
+            "try:\n    L.load()\nexcept ImportError as e:\n    print('raised', e)\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.startswith("raised") and "no CPU fallback" in r.stdout

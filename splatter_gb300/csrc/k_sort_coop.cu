@@ -6,8 +6,9 @@
 // tile — dominates.  Here every CTA is resident (cooperative launch, two 512-thread CTAs per SM) and
 // owns one contiguous segment of the input; each 8-bit pass is:
 //   1. count: the segment's digit histogram -> cnt[digit][cta]                       (global)
-//   2. bounded grid barrier; CTA d scans digit row d in place (exclusive prefix over CTAs) and
-//      writes the row total; bounded grid barrier
+//   2. bounded grid barrier; the digit rows, dealt round robin over the CTAs, are scanned in place
+//      (exclusive prefix over CTAs, by one warp or, for a few CTAs, one thread per row) and their
+//      totals written; bounded grid barrier
 //   3. offsets: each CTA reads its column of prefixes and the 256 totals (global digit bases)
 //   4. scatter, sub-tile by sub-tile (4096 keys): warp-level multisplit ranking (digit match by eight
 //      ballots),
@@ -26,7 +27,9 @@ constexpr int CS_NQ = CS_THREADS / 256;        // threads per digit in the per-d
 constexpr int CS_WPQ = CS_WARPS / CS_NQ;       // warps summed by one of those threads
 constexpr int CS_KPT = 8;
 constexpr int CS_TILE = CS_THREADS * CS_KPT;  // 4096 keys per sub-tile
+constexpr int CS_SCAN_RUN = 16;               // count-table entries per lane in the row scan: grids <= 512
 static_assert(CS_THREADS % 256 == 0, "the per-digit phases map 256 digits onto groups of threads");
+static_assert(CS_THREADS == 512 && CS_WARPS == 16, "the sub-tile scan maps digit t / 2 and 8 warps to thread t");
 
 struct CoopSmem {
     uint32_t buf[CS_TILE];             // keys of the sub-tile in digit order
@@ -90,26 +93,146 @@ __device__ __forceinline__ uint32_t scan256(uint32_t v, uint32_t* scan, uint32_t
     return pre + x - v;
 }
 
+// Ranks one sub-tile's keys (key[j] is element wb + 32 j, valid below `end`) by the digit at `shift`
+// (warp-level multisplit: equal digits keep their input order) and stages keys and values in digit
+// order in sm.buf / sm.vbuf; sm.dstart / sm.tcount receive the sub-tile's digit offsets and counts.
+// Every thread of the CTA calls it; it ends with a CTA barrier.
+__device__ __forceinline__ void stage_subtile(CoopSmem& sm, const uint32_t (&key)[CS_KPT], const uint32_t (&val)[CS_KPT],
+                                              uint32_t wb, uint32_t end, int shift, uint32_t lt) {
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sm.wcnt[w][lane + 32 * k] = 0u;
+    __syncwarp();
+    uint32_t pos[CS_KPT];
+#pragma unroll
+    for (int j = 0; j < CS_KPT; ++j) {
+        const uint32_t e = wb + 32u * j;
+        const bool valid = e < end;
+        const uint32_t d = (key[j] >> shift) & 255u;
+        const uint32_t peers = match_digit(d, valid);
+        uint32_t cur = 0;
+        if (valid) cur = sm.wcnt[w][d];
+        __syncwarp();
+        if (valid && lane == 31u - __clz(peers)) sm.wcnt[w][d] = cur + __popc(peers);
+        __syncwarp();
+        pos[j] = cur + __popc(peers & lt);
+    }
+    __syncthreads();
+    // One exclusive scan of the count table in (digit, warp) order gives every (warp, digit) its
+    // first position in the sub-tile: thread t owns digit t / 2 and half of the warps; the thread
+    // sums go through a warp scan and the warp totals.  dstart / tcount: each digit's start and count.
+    {
+        constexpr int HW = CS_WARPS / 2;
+        const uint32_t d = tid >> 1, w0 = (tid & 1u) * HW;
+        uint32_t c8[HW], sum = 0;
+#pragma unroll
+        for (int k = 0; k < HW; ++k) {
+            c8[k] = sm.wcnt[w0 + k][d];
+            sum += c8[k];
+        }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31u) sm.scan[w] = x;
+        __syncthreads();
+        uint32_t wpre = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < (uint32_t)CS_WARPS; ++i) wpre += i < w ? sm.scan[i] : 0u;
+        const uint32_t excl = wpre + x - sum;
+        uint32_t run = excl;
+#pragma unroll
+        for (int k = 0; k < HW; ++k) {
+            sm.wcnt[w0 + k][d] = run;
+            run += c8[k];
+        }
+        const uint32_t first = __shfl_xor_sync(FULL_MASK, excl, 1);  // the digit's other half
+        if (tid & 1u) {
+            sm.dstart[d] = first;
+            sm.tcount[d] = run - first;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < CS_KPT; ++j) {
+        const uint32_t e = wb + 32u * j;
+        if (e < end) {
+            const uint32_t d = (key[j] >> shift) & 255u;
+            const uint32_t p = pos[j] + sm.wcnt[w][d];
+            sm.buf[p] = key[j];
+            sm.vbuf[p] = val[j];
+        }
+    }
+    __syncthreads();
+}
+
 // keys0 -> keys1 -> keys0 ... for `passes` passes starting at bit `shift0`; vals likewise (both value
 // buffers are real; with iota_first the values read by pass 0 are the input positions instead of
-// vals0).  The result of pass p is in keys1/vals1 for even p and keys0/vals0 for odd p.
+// vals0).  The result of pass p is in keys1/vals1 for even p and keys0/vals0 for odd p (for at most
+// one sub-tile of keys only the last pass's buffers are written).
 __global__ void __launch_bounds__(CS_THREADS, 2)
     k_sort_coop(uint32_t* keys0, uint32_t* keys1, uint32_t* vals0, uint32_t* vals1, int iota_first,
                 const uint32_t* n_ptr, uint32_t n_cap, int passes, int shift0, uint32_t* cnt /*[256][Gp] + tot[256]*/,
                 uint32_t* bar, uint32_t spin_limit, uint32_t* err) {
-    // cnt rows: [256][Gp], Gp = gridDim rounded up to a multiple of 4 so rows are 16-byte aligned
+    // cnt rows: [256][Gp], Gp = the working CTAs rounded up to a multiple of 4 (16-byte rows)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CoopSmem& sm = *reinterpret_cast<CoopSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, w = tid >> 5;
-    const uint32_t G = gridDim.x, c = blockIdx.x;
+    const uint32_t c = blockIdx.x;
+    const uint32_t n = min(*n_ptr, n_cap);
+    // Contiguous segments, 256-aligned and at least one sub-tile long.  The live count is read on
+    // the device (a captured graph replays with any count up to n_cap), so the grid is sized for
+    // n_cap; CTAs past the last segment leave before the first barrier, which counts only the G
+    // CTAs that work: a small sort pays for a few CTAs' barriers, not the whole grid's.
+    uint32_t seg = (n + gridDim.x - 1) / gridDim.x;
+    seg = max((seg + 255u) & ~255u, (uint32_t)CS_TILE);
+    const uint32_t G = (n + seg - 1) / seg;
+    if (c >= G) return;
+    const uint32_t lt = lanemask_lt();
+    if (G == 1u) {
+        // n <= CS_TILE: one sub-tile.  Every pass ranks and stages it in shared memory (no count
+        // table, no grid barriers); the keys are read once and written once, to the buffers the last
+        // pass writes (keys1/vals1 after an odd number of passes, keys0/vals0 after an even one).
+        uint32_t key[CS_KPT], val[CS_KPT];
+        const uint32_t wb = w * (32u * CS_KPT) + lane;
+#pragma unroll
+        for (int j = 0; j < CS_KPT; ++j) {
+            const uint32_t e = wb + 32u * j;
+            const bool ok = e < n;
+            key[j] = ok ? __ldcg(keys0 + e) : 0u;
+            val[j] = ok ? (iota_first ? e : __ldcg(vals0 + e)) : 0u;
+        }
+        for (int p = 0; p < passes; ++p) {
+            stage_subtile(sm, key, val, wb, n, shift0 + 8 * p, lt);
+            if (p + 1 < passes) {
+#pragma unroll
+                for (int j = 0; j < CS_KPT; ++j) {
+                    const uint32_t e = wb + 32u * j;
+                    if (e < n) {
+                        key[j] = sm.buf[e];
+                        val[j] = sm.vbuf[e];
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        uint32_t* kout = (passes & 1) ? keys1 : keys0;
+        uint32_t* vout = (passes & 1) ? vals1 : vals0;
+#pragma unroll
+        for (int j = 0; j < CS_KPT; ++j) {
+            const uint32_t i = tid + CS_THREADS * j;
+            if (i < n) {
+                kout[i] = sm.buf[i];
+                vout[i] = sm.vbuf[i];
+            }
+        }
+        return;
+    }
     const uint32_t Gp = (G + 3u) & ~3u;  // padded row stride of cnt (16-byte rows)
     uint32_t* tot = cnt + (size_t)256 * Gp;  // per-digit totals of a pass
-    const uint32_t n = min(*n_ptr, n_cap);
-    // contiguous segments, 256-aligned
-    uint32_t seg = (n + G - 1) / G;
-    seg = (seg + 255u) & ~255u;
-    const uint32_t s_begin = min(c * seg, n), s_end = min(s_begin + seg, n);
-    const uint32_t lt = lanemask_lt();
+    const uint32_t s_begin = c * seg, s_end = min(s_begin + seg, n);
     for (int p = 0; p < passes; ++p) {
         const int shift = shift0 + 8 * p;
         const uint32_t* kin = (p & 1) ? keys1 : keys0;
@@ -165,34 +288,56 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
         }
         __syncthreads();
         grid_barrier(bar, G, spin_limit, err);
-        // ---- 3a. distributed scan: CTA c turns the digit rows d = c, c + G, ... of cnt[d][0..G) into
-        //          their exclusive prefixes over CTAs and writes the row totals to tot[d] ----
-        for (uint32_t d = c; d < 256u; d += G) {  // uniform across the CTA
-            uint32_t* row = cnt + (size_t)d * Gp;
-            uint32_t carry = 0;
-            for (uint32_t k0 = 0; k0 < G; k0 += CS_THREADS) {  // uniform across the CTA
-                const uint32_t k = k0 + tid;
-                const uint32_t v = k < G ? __ldcg(row + k) : 0u;
-                uint32_t x = v;
+        // ---- 3a. distributed scan: digit row d of cnt[d][0..G) becomes its exclusive prefix over
+        //          the CTAs and its total goes to tot[d].  The rows are dealt round robin over the
+        //          CTAs, so every row's loads are in flight at once (one L2 round trip): with at most
+        //          CS_SCAN_RUN CTAs one thread scans a row (d = tid * G + c), otherwise one warp
+        //          (d = w * G + c), each lane a run of consecutive entries, a warp scan of the run
+        //          sums giving the runs' offsets ----
+        if (G <= (uint32_t)CS_SCAN_RUN) {
+            const uint32_t d = tid * G + c;
+            if (d < 256u) {
+                uint32_t* row = cnt + (size_t)d * Gp;
+                uint32_t v[CS_SCAN_RUN];
+#pragma unroll
+                for (int j = 0; j < CS_SCAN_RUN; ++j) v[j] = (uint32_t)j < G ? __ldcg(row + j) : 0u;
+                uint32_t run = 0;
+#pragma unroll
+                for (int j = 0; j < CS_SCAN_RUN; ++j) {
+                    if ((uint32_t)j < G) row[j] = run;
+                    run += v[j];
+                }
+                tot[d] = run;
+            }
+        } else {
+            const uint32_t d = w * G + c;  // warp-uniform
+            if (d < 256u) {
+                const uint32_t per = (G + 31u) / 32u;  // entries per lane, <= CS_SCAN_RUN
+                uint32_t* row = cnt + (size_t)d * Gp;
+                const uint32_t k0 = lane * per;
+                uint32_t v[CS_SCAN_RUN];
+                uint32_t sum = 0;
+#pragma unroll
+                for (int j = 0; j < CS_SCAN_RUN; ++j) {
+                    const uint32_t k = k0 + (uint32_t)j;
+                    v[j] = ((uint32_t)j < per && k < G) ? __ldcg(row + k) : 0u;
+                    sum += v[j];
+                }
+                uint32_t x = sum;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
                     if (lane >= (uint32_t)o) x += y;
                 }
-                if (lane == 31) sm.scan[w] = x;
-                __syncthreads();
-                uint32_t wpre = 0, ctot = 0;
+                uint32_t run = x - sum;
 #pragma unroll
-                for (uint32_t i = 0; i < (uint32_t)CS_WARPS; ++i) {
-                    const uint32_t t = sm.scan[i];
-                    wpre += i < w ? t : 0u;
-                    ctot += t;
+                for (int j = 0; j < CS_SCAN_RUN; ++j) {
+                    const uint32_t k = k0 + (uint32_t)j;
+                    if ((uint32_t)j < per && k < G) row[k] = run;
+                    run += v[j];
                 }
-                __syncthreads();
-                if (k < G) row[k] = carry + wpre + x - v;
-                carry += ctot;
+                if (lane == 31u) tot[d] = x;
             }
-            if (tid == 0) tot[d] = carry;
         }
         grid_barrier(bar, G, spin_limit, err);
         // ---- 3b. offsets: this CTA's column of prefixes plus the global digit bases ----
@@ -213,10 +358,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
         // ---- 4. scatter, sub-tile by sub-tile ----
         for (uint32_t tb = s_begin; tb < s_end; tb += CS_TILE) {
             const uint32_t tn = min((uint32_t)CS_TILE, s_end - tb);
-#pragma unroll
-            for (int k = 0; k < 8; ++k) sm.wcnt[w][lane + 32 * k] = 0u;
-            __syncwarp();
-            uint32_t key[CS_KPT], pos[CS_KPT], val[CS_KPT];
+            uint32_t key[CS_KPT], val[CS_KPT];
             const uint32_t wb = tb + w * (32u * CS_KPT) + lane;  // warp w owns 32 x CS_KPT consecutive keys
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
@@ -225,66 +367,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
                 key[j] = ok ? __ldcg(kin + e) : 0u;
                 val[j] = ok ? (iota ? e : __ldcg(vin + e)) : 0u;
             }
-#pragma unroll
-            for (int j = 0; j < CS_KPT; ++j) {
-                const uint32_t e = wb + 32u * j;
-                const bool valid = e < tb + tn;
-                const uint32_t d = (key[j] >> shift) & 255u;
-                const uint32_t peers = match_digit(d, valid);
-                uint32_t cur = 0;
-                if (valid) cur = sm.wcnt[w][d];
-                __syncwarp();
-                if (valid && lane == 31u - __clz(peers)) sm.wcnt[w][d] = cur + __popc(peers);
-                __syncwarp();
-                pos[j] = cur + __popc(peers & lt);
-            }
-            __syncthreads();
-            // per digit: exclusive prefix over the warps (thread (d, q) handles warps CS_WPQ*q ..)
-            {
-                const uint32_t d = tid & 255u, q = tid >> 8;
-                uint32_t s = 0;
-#pragma unroll
-                for (int k = 0; k < CS_WPQ; ++k) {
-                    const uint32_t v = sm.wcnt[CS_WPQ * q + k][d];
-                    sm.wcnt[CS_WPQ * q + k][d] = s;
-                    s += v;
-                }
-                sm.part[q][d] = s;
-            }
-            __syncthreads();
-            {
-                const uint32_t d = tid & 255u, q = tid >> 8;
-                uint32_t add = 0;
-#pragma unroll
-                for (uint32_t k = 0; k < (uint32_t)CS_NQ; ++k) add += k < q ? sm.part[k][d] : 0u;
-                if (add) {
-#pragma unroll
-                    for (int k = 0; k < CS_WPQ; ++k) sm.wcnt[CS_WPQ * q + k][d] += add;
-                }
-            }
-            uint32_t tc = 0;
-            if (tid < 256) {
-#pragma unroll
-                for (int q = 0; q < CS_NQ; ++q) tc += sm.part[q][tid];
-            }
-            uint32_t tt;
-            const uint32_t ds = scan256(tc, sm.scan, &tt);  // contains __syncthreads
-            if (tid < 256) {
-                sm.dstart[tid] = ds;
-                sm.tcount[tid] = tc;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < CS_KPT; ++j) {
-                const uint32_t e = wb + 32u * j;
-                if (e < tb + tn) {
-                    const uint32_t d = (key[j] >> shift) & 255u;
-                    const uint32_t p = pos[j] + sm.dstart[d] + sm.wcnt[w][d];
-                    sm.buf[p] = key[j];
-                    sm.vbuf[p] = val[j];
-                }
-            }
-            __syncthreads();
+            stage_subtile(sm, key, val, wb, tb + tn, shift, lt);
             // keys and values leave together: each digit's run is consecutive in the output
 #pragma unroll
             for (int j = 0; j < CS_KPT; ++j) {
@@ -318,6 +401,7 @@ int sort_coop_grid() {
         cudaFuncSetAttribute(k_sort_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CoopSmem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sort_coop, CS_THREADS, sizeof(CoopSmem));
         g_cs_grid = sms * (per > 0 ? per : 1);
+        if (g_cs_grid > 32 * CS_SCAN_RUN) g_cs_grid = 32 * CS_SCAN_RUN;
     }
     return g_cs_grid;
 }

@@ -257,40 +257,51 @@ SPL_API int spl_activate_splats_backward(uint64_t n, const float* quaternions, c
 SPL_API int spl_renderer_copy_record_gradients(spl_renderer* r, float* dst_device, uint64_t capacity, void* stream);
 
 /* ---- device sort (radixSortB/radixSortC, shaders.wgsl:338-498) --------------------------------- */
-/* Stable LSD onesweep sort of `count` (key, value) pairs on the device: keys_in/values_in are
- * sorted into keys_out/values_out by the low `key_bits` bits of the key (8, 16, 24 or 32).
+/* Stable LSD radix sort of `count` (key, value) pairs on the device: keys_in/values_in are
+ * sorted into keys_out/values_out by the low `key_bits` bits of the key (8, 16, 24 or 32), all
+ * digit passes in one cooperative launch (the whole device; do not overlap it with a frame).
  * Uses the renderer's scratch (count <= max_splat_count).  Asynchronous on `stream`. */
 SPL_API int spl_sort_pairs(spl_renderer* r, const uint32_t* keys_in, const uint32_t* values_in, uint32_t* keys_out,
                    uint32_t* values_out, uint64_t count, uint32_t key_bits, void* stream);
 
 /* ---- sorting without allocation -------------------------------------------------------------------- */
 /* No counterpart in the reference: an addition for callers that cannot allocate device memory when
- * they sort — hosts that give all device memory to their own pool up front, code running while a
- * CUDA graph is captured, plug-ins that may only touch the buffers they are handed.
- * spl_sort_pairs_no_alloc is spl_sort_pairs (same stable result, same kernels) without a renderer:
- * its scratch is a static device array the library reserves on every device that loads it (2.6 MB,
- * held until the process exits), and it calls no allocator.  At most SPL_NO_ALLOC_MAX_PAIRS pairs
- * per call (larger counts return SPL_ERR_INVALID).  All calls on a device share that scratch: calls
- * whose GPU work overlaps race and give wrong results, so order them on one stream.  The first call
- * on a device looks up the scratch address (cudaGetSymbolAddress); make it before any stream
- * capture.  Inputs and outputs must not overlap.  Asynchronous on `stream`. */
+ * they sort — hosts that give all device memory to their own pool up front (a cudaMalloc would fail
+ * or bypass their accounting), plug-ins that may only touch the buffers they are handed, and loops
+ * that must not take cudaMalloc's implicit device-wide synchronisation.
+ * spl_sort_pairs_no_alloc gives the same stable result as spl_sort_pairs, through the onesweep passes
+ * (spl_sort_pairs runs the cooperative sort), without a renderer: its scratch is a static device
+ * array the library reserves on every device that loads it (2.6 MB, held until the process exits),
+ * and it calls no allocator.  At most SPL_NO_ALLOC_MAX_PAIRS pairs per call (larger counts return
+ * SPL_ERR_INVALID).  All calls on a device share that scratch and its contents persist between
+ * calls: calls whose GPU work overlaps race and give wrong results, so order them on one stream.
+ * The first call on a device looks up the scratch address (cudaGetSymbolAddress) with that device
+ * current; make it before any stream capture.  Only the device's primary context is supported (the
+ * address is cached per device ordinal; after cudaDeviceReset it is stale).  Inputs and outputs
+ * must not overlap.  Asynchronous on `stream`. */
 #define SPL_NO_ALLOC_MAX_PAIRS 262144u
 SPL_API int spl_sort_pairs_no_alloc(const uint32_t* keys_in, const uint32_t* values_in, uint32_t* keys_out,
                                     uint32_t* values_out, uint64_t count, uint32_t key_bits, void* stream);
+/* Status of the last spl_sort_pairs_no_alloc on the current device: waits for `stream` (the stream
+ * that call used), then reads the scratch's device error word into *device_error (may be NULL;
+ * bit 1 = a bounded look-back wait ran out, so the output is not sorted) and returns
+ * SPL_ERR_LOOKBACK_TIMEOUT when it is set, SPL_OK otherwise.  Allocates nothing.  The word is
+ * cleared by the next sort call with a non-zero count. */
+SPL_API int spl_sort_pairs_no_alloc_status(void* stream, uint32_t* device_error);
 
 /* ---- diagnostics ----------------------------------------------------------------------------------- */
-/* Stage timing with CUDA events on the launching streams (off by default).  When enabled, each
- * render_frame records events around its stages; spl_renderer_stage_times waits for the last frame
- * and writes SPL_STAGE_COUNT durations in milliseconds, indexed by SPL_STAGE_*.  The vertex stage
- * runs on a side stream and overlaps the depth sort, so the stage times may sum to more than the
- * frame time. */
-#define SPL_STAGE_CULL 0       /* cull + key + histogram + compaction */
+/* Stage timing with CUDA events on the launching stream (off by default).  When enabled, each
+ * render_frame records events between its stages; spl_renderer_stage_times waits for the last frame
+ * and writes SPL_STAGE_COUNT durations in milliseconds, indexed by SPL_STAGE_*.  The stages run one
+ * after another on the frame's stream, so they add up to the frame time. */
+#define SPL_STAGE_CULL 0       /* frame start, cull + key + ordered compaction */
 #define SPL_STAGE_PREPROCESS 1 /* vertex stage: colour, conic, rectangle records */
-#define SPL_STAGE_DEPTH_SORT 2 /* four onesweep passes over the visible keys */
-#define SPL_STAGE_BIN 3        /* tile binning */
-#define SPL_STAGE_PAIR_SORT 4  /* onesweep passes over the tile ids */
+#define SPL_STAGE_DEPTH_SORT 2 /* the stable depth sort of the visible keys (one cooperative launch,
+                                  or one onesweep launch per digit pass) */
+#define SPL_STAGE_BIN 3        /* tile-range clear + tile binning */
+#define SPL_STAGE_PAIR_SORT 4  /* the stable sort of the (tile, splat) pairs by tile id */
 #define SPL_STAGE_RANGES 5     /* per-tile list ranges */
-#define SPL_STAGE_RASTER 6     /* tile raster + blend */
+#define SPL_STAGE_RASTER 6     /* tile order + tile raster + blend */
 #define SPL_STAGE_FRAME 7      /* whole frame on the main stream */
 #define SPL_STAGE_COUNT 8
 SPL_API int spl_renderer_set_profiling(spl_renderer* r, int enable);

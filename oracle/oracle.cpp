@@ -948,6 +948,7 @@ struct GradCtx {
     int W, H, TX, TY;
     size_t n;
     std::vector<double> c, q, s, a, sh, target;
+    std::vector<double> gimg;  // when set: dL/dC per pixel and channel used by the backward instead of 2 (C - target)
     std::vector<uint32_t> order, key;   // drawn splats in depth order, and their FP32 keys
     std::vector<int64_t> pos_of;        // splat -> draw position (-1: not drawn)
     std::vector<GRec> rec;              // per draw position
@@ -1141,6 +1142,18 @@ OAPI void oracle_grad_pin_records(void* h, const float* recs16, const uint32_t* 
     rebuild_tiles(g);
 }
 
+// The backward's upstream gradient dL/dC (H x W x 3) taken as given instead of 2 (C - target) of the
+// FP64 frame: e.g. the FP32 frame's own 2 (C32 - target), so that the FP64 backward and a renderer's
+// FP32 backward start from the same upstream gradient and differ only by their own arithmetic.  NULL
+// restores 2 (C - target).
+OAPI void oracle_grad_set_image_gradient(void* h, const double* grad_image) {
+    GradCtx& g = *(GradCtx*)h;
+    if (grad_image)
+        g.gimg.assign(grad_image, grad_image + 3 * (size_t)g.W * g.H);
+    else
+        g.gimg.clear();
+}
+
 // Full-frame FP64 loss; grads (n x 59) receive the analytic FP64 gradient (zero for splats not drawn).
 OAPI double oracle_grad_loss_ex(void* h, double* grads, double* image_out, int threads, double* rec_grads_out,
                                 uint32_t* order_out);
@@ -1179,7 +1192,7 @@ OAPI double oracle_grad_loss_ex(void* h, double* grads, double* image_out, int t
                     for (int ch = 0; ch < 3; ++ch) {
                         const double d = C[ch] - g.target[3 * pix + ch];
                         loss_t[tid] += d * d;
-                        gC[ch] = 2.0 * d;
+                        gC[ch] = g.gimg.empty() ? 2.0 * d : g.gimg[3 * pix + ch];
                         if (image_out) image_out[4 * pix + ch] = C[ch];
                     }
                     if (image_out) image_out[4 * pix + 3] = Tf;
@@ -1300,32 +1313,41 @@ OAPI void oracle_grad_jacobian(void* h, uint64_t k, double* J) {
     }
 }
 
-// Central difference of the loss in parameter `param` (0..58) of splat k with step hstep.  Returns 1
-// and writes *fd when nothing discrete changes under +-hstep, 0 otherwise (excluded).
-OAPI int oracle_grad_fd(void* h, uint64_t k, int param, double hstep, double* fd) {
-    GradCtx& g = *(GradCtx*)h;
+namespace {
+// Central difference of the loss between two parameter vectors of splat k (59 activated values
+// each): (loss(p[0]) - loss(p[1])) / denom, re-rendering only the tiles the splat touches.  Returns
+// 0 (excluded) when anything discrete differs between the two or from the base frame; a splat this
+// frame does not draw has difference 0 unless a step would draw it.
+int fd_between(GradCtx& g, uint64_t k, const double* const p[2], double denom, double* fd) {
     *fd = 0.0;
-    if (g.pos_of[k] < 0) return 0;
+    if (k >= g.n) return 0;
+    if (g.pos_of[k] < 0) {
+        // not drawn in this frame: the difference is 0 when it stays undrawn under both steps (culled,
+        // or a key the mode does not draw), excluded when a step would draw it
+        for (int sgn = 0; sgn < 2; ++sgn) {
+            float cf[3] = {(float)p[sgn][0], (float)p[sgn][1], (float)p[sgn][2]};
+            uint32_t kk;
+            uint8_t vis;
+            oracle_cull_keys(&g.u, g.cfg.depth_sorting, cf, 1, &kk, &vis);
+            const bool drawn = vis && !(g.cfg.depth_sorting == 2 && kk == 0xFFFFFFFFu) &&
+                               !(g.cfg.depth_sorting == 3 && (kk >> 24) == 0xFFu);
+            if (drawn) return 0;
+        }
+        return 1;
+    }
     const uint32_t pos = (uint32_t)g.pos_of[k];
-    double base[NPARAM];
-    for (int i = 0; i < 3; ++i) base[i] = g.c[3 * k + i];
-    for (int i = 0; i < 4; ++i) base[3 + i] = g.q[4 * k + i];
-    for (int i = 0; i < 3; ++i) base[7 + i] = g.s[3 * k + i];
-    base[10] = g.a[k];
-    for (int i = 0; i < 48; ++i) base[11 + i] = g.sh[48 * k + i];
     GRec rr[2];
     for (int sgn = 0; sgn < 2; ++sgn) {
-        double p[NPARAM];
-        std::memcpy(p, base, sizeof(p));
-        p[param] += sgn == 0 ? hstep : -hstep;
-        if (param < 3) {  // the FP32 depth key (and culling) must not change
-            float cf[3] = {(float)p[0], (float)p[1], (float)p[2]};
+        const double* q = p[sgn];
+        if (q[0] != g.c[3 * k] || q[1] != g.c[3 * k + 1] || q[2] != g.c[3 * k + 2]) {
+            // the FP32 depth key (and culling) must not change
+            float cf[3] = {(float)q[0], (float)q[1], (float)q[2]};
             uint32_t kk;
             uint8_t vis;
             oracle_cull_keys(&g.u, g.cfg.depth_sorting, cf, 1, &kk, &vis);
             if (!vis || kk != g.key[pos]) return 0;
         }
-        rr[sgn] = rec_of_splat(g, k, p);
+        rr[sgn] = rec_of_splat(g, k, q);
         if (!rr[sgn].valid) return 0;
     }
     const GRec& r0 = g.rec[pos];
@@ -1364,8 +1386,43 @@ OAPI int oracle_grad_fd(void* h, uint64_t k, int param, double hstep, double* fd
         }
         if (sig[0] != sig[1]) return 0;
     }
-    *fd = (loss[0] - loss[1]) / (2.0 * hstep);
+    *fd = (loss[0] - loss[1]) / denom;
     return 1;
+}
+
+void base_params(const GradCtx& g, uint64_t k, double* base) {
+    for (int i = 0; i < 3; ++i) base[i] = g.c[3 * k + i];
+    for (int i = 0; i < 4; ++i) base[3 + i] = g.q[4 * k + i];
+    for (int i = 0; i < 3; ++i) base[7 + i] = g.s[3 * k + i];
+    base[10] = g.a[k];
+    for (int i = 0; i < 48; ++i) base[11 + i] = g.sh[48 * k + i];
+}
+}  // namespace
+
+// Central difference of the loss in parameter `param` (0..58) of splat k with step hstep.  Returns 1
+// and writes *fd when nothing discrete changes under +-hstep, 0 otherwise (excluded).
+OAPI int oracle_grad_fd(void* h, uint64_t k, int param, double hstep, double* fd) {
+    GradCtx& g = *(GradCtx*)h;
+    *fd = 0.0;
+    if (k >= g.n || param < 0 || param >= NPARAM) return 0;
+    double pp[NPARAM], pm[NPARAM];
+    base_params(g, k, pp);
+    std::memcpy(pm, pp, sizeof(pp));
+    pp[param] += hstep;
+    pm[param] -= hstep;
+    const double* const p[2] = {pp, pm};
+    return fd_between(g, k, p, 2.0 * hstep, fd);
+}
+
+// The same difference between two explicit parameter vectors of splat k (59 activated values each,
+// centre 3, rotation 4, scale 3, opacity, SH 48), divided by `denom`: for steps in parameters that
+// the loss sees only through an activation moving several of these at once (a raw log-scale moves
+// all three scales when its clamp is active, a raw quaternion component all four rotation values).
+OAPI int oracle_grad_fd_params(void* h, uint64_t k, const double* p_plus, const double* p_minus, double denom,
+                               double* fd) {
+    GradCtx& g = *(GradCtx*)h;
+    const double* const p[2] = {p_plus, p_minus};
+    return fd_between(g, k, p, denom, fd);
 }
 
 // Splats whose gradient depends on a decision that the FP32 frame and the FP64 frame take

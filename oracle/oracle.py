@@ -14,6 +14,7 @@ from . import build_oracle
 __all__ = [
     "lib", "uniforms", "cull_keys", "draw_list", "preprocess", "raster", "raster_work", "render", "load_transform",
     "cpu_sort_fallback", "cpu_frame_timed", "expf", "GradContext", "OCFG", "UNIFORM_DTYPE", "config_struct",
+    "RAW_SLOT_COLUMNS", "raw_slots", "activate64", "scene64", "raw_gradients64",
 ]
 
 _lib = None
@@ -190,6 +191,57 @@ def load_transform(records):
     return out
 
 
+# Raw parameters in the 59-slot order of the gradient context (centre 3, quaternion 4, log-scale 3,
+# opacity logit, SH 48): their columns in the 62-float file record (scene.rs:15-24).
+RAW_SLOT_COLUMNS = np.array([0, 1, 2, 58, 59, 60, 61, 55, 56, 57, 54] + list(range(6, 54)))
+
+
+def raw_slots(records):
+    """(N, 59) raw parameters of (N, 62) file records in slot order, as float64."""
+    return np.asarray(records, np.float64).reshape(-1, 62)[:, RAW_SLOT_COLUMNS]
+
+
+def activate64(raw):
+    """The loader's transform (scene.rs:225-250) in FP64 on (N, 59) raw slots: the activated slots
+    (centre, unit rotation, scale = exp(clamp(log-scale, mean -+ 5)), opacity = sigmoid(logit), SH)."""
+    raw = np.asarray(raw, np.float64).reshape(-1, 59)
+    out = raw.copy()
+    q = raw[:, 3:7]
+    out[:, 3:7] = q / np.sqrt((q * q).sum(1, keepdims=True))
+    ls = raw[:, 7:10]
+    avg = ls.sum(1, keepdims=True) / 3.0
+    out[:, 7:10] = np.exp(np.clip(ls, avg - 5.0, avg + 5.0))
+    out[:, 10] = 1.0 / (1.0 + np.exp(-raw[:, 10]))
+    return out
+
+
+def scene64(activated):
+    """The gradient context's scene dict of (N, 59) activated slots."""
+    a = np.asarray(activated, np.float64)
+    return {"center": a[:, 0:3], "rotation": a[:, 3:7], "scale": a[:, 7:10], "alpha": a[:, 10], "sh": a[:, 11:59]}
+
+
+def raw_gradients64(raw, grads):
+    """Chain rule of activate64: gradients of the activated slots (N, 59) -> gradients of the raw slots."""
+    raw = np.asarray(raw, np.float64).reshape(-1, 59)
+    g = np.array(grads, np.float64).reshape(-1, 59)
+    out = g.copy()
+    q = raw[:, 3:7]
+    nq = np.sqrt((q * q).sum(1, keepdims=True))
+    r = q / nq
+    gr = g[:, 3:7]
+    out[:, 3:7] = (gr - (gr * r).sum(1, keepdims=True) * r) / nq
+    ls = raw[:, 7:10]
+    avg = ls.sum(1, keepdims=True) / 3.0
+    clamped = (ls < avg - 5.0) | (ls > avg + 5.0)
+    s = np.exp(np.clip(ls, avg - 5.0, avg + 5.0))
+    gs = g[:, 7:10] * s
+    out[:, 7:10] = np.where(clamped, 0.0, gs) + np.where(clamped, gs, 0.0).sum(1, keepdims=True) / 3.0
+    a = 1.0 / (1.0 + np.exp(-raw[:, 10]))
+    out[:, 10] = g[:, 10] * a * (1.0 - a)
+    return out
+
+
 def cpu_frame_timed(u, cfg, scene, threads=8, tile_stride=1):
     """The reference's CPU path for one frame (CPU depth-sort fallback + restated vertex/fragment/blend),
     timed per stage; returns (image, V, (t_sort, t_vertex, t_raster) seconds)."""
@@ -232,6 +284,10 @@ class GradContext:
             L.oracle_grad_loss.argtypes = [P, P, P, ctypes.c_int]
             L.oracle_grad_fd.restype = ctypes.c_int
             L.oracle_grad_fd.argtypes = [P, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, P]
+            L.oracle_grad_set_image_gradient.restype = None
+            L.oracle_grad_set_image_gradient.argtypes = [P, P]
+            L.oracle_grad_fd_params.restype = ctypes.c_int
+            L.oracle_grad_fd_params.argtypes = [P, ctypes.c_uint64, P, P, ctypes.c_double, P]
             L.oracle_grad_pin_records.restype = None
             L.oracle_grad_pin_records.argtypes = [P, P, P, ctypes.c_uint64]
             L.oracle_grad_jacobian.restype = None
@@ -288,6 +344,22 @@ class GradContext:
     def fd(self, k, param, h=1e-4):
         out = np.zeros(1, np.float64)
         ok = lib().oracle_grad_fd(self._h, int(k), int(param), float(h), _p(out))
+        return bool(ok), float(out[0])
+
+    def set_image_gradient(self, grad_image):
+        """Use grad_image (H, W, 3) as dL/dC in the backward (None: 2 (C - target) of the FP64 frame)."""
+        if grad_image is None:
+            lib().oracle_grad_set_image_gradient(self._h, None)
+            return
+        self._gimg = np.ascontiguousarray(grad_image, np.float64).reshape(self.H, self.W, 3)
+        lib().oracle_grad_set_image_gradient(self._h, _p(self._gimg))
+
+    def fd_params(self, k, p_plus, p_minus, denom):
+        """(loss(p_plus) - loss(p_minus)) / denom for splat k's 59 activated parameters; (ok, value)."""
+        pp = np.ascontiguousarray(p_plus, np.float64).reshape(self.NPARAM)
+        pm = np.ascontiguousarray(p_minus, np.float64).reshape(self.NPARAM)
+        out = np.zeros(1, np.float64)
+        ok = lib().oracle_grad_fd_params(self._h, int(k), _p(pp), _p(pm), float(denom), _p(out))
         return bool(ok), float(out[0])
 
     def close(self):

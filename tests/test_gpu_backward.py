@@ -134,7 +134,7 @@ def frame(request):
           + ("" if cov else f"; FP32 ellipse within 1e-4 of FP64 for {int(well[drawn].sum())}"))
     nparam = 11 + 3 * (cfg.spherical_harmonics_order + 1) ** 2
     yield dict(r=r, ctx=ctx, loss=loss, loss64=loss64, g=g, ref=ref, amb=amb, drawn=drawn, drawn_all=drawn_all,
-               nparam=nparam, well=drawn[well[drawn]], cov=cov, img=img, img64=img64, npix=npix)
+               nparam=nparam, well=drawn[well[drawn]], cov=cov, rect=rect, img=img, img64=img64, npix=npix)
     ctx.close()
 
 
@@ -239,7 +239,13 @@ def test_parameter_gradients_match_finite_differences(frame):
     print(f"vs FP64 FD: 256 params ({excluded} excluded: discrete change under +-h), "
           f"{100 * np.mean(rel_fd <= REL_TOL):.1f}% within {REL_TOL}, max {rel_fd.max():.2e}; "
           f"FP64 reference vs FD max {rel_ref_fd.max():.2e}")
-    if frame["cov"]:
+    if frame["cov"] and frame["rect"]:
+        # the default configuration: every parameter
+        assert np.all(rel_ref_fd <= REL_TOL)
+        assert np.all(rel_fd <= REL_TOL)
+    elif frame["cov"]:
+        # axis-aligned squares: a square's side is the larger rotated semi-axis, max(|a|, |b|), whose
+        # derivative switches where the two meet; 255 of 256 within 1e-3 (max 1.25e-3) measured
         assert np.mean(rel_ref_fd <= REL_TOL) >= 0.99
         assert np.mean(rel_fd <= REL_TOL) >= 0.99
     else:

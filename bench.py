@@ -58,7 +58,7 @@ def parse_args(argv=None):
     p.add_argument("--no-loading", action="store_true", help="skip the splat-file loading leg")
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-requests", type=int, default=800, help="closed-loop requests per loop")
-    p.add_argument("--serve-rates", default="250,1000,2000", help="Poisson arrival rates (req/s)")
+    p.add_argument("--serve-rates", default="50,250,1000,2000", help="Poisson arrival rates (req/s)")
     p.add_argument("--serve-seconds", type=float, default=1.0, help="arrival span per rate")
     p.add_argument("--serve-evict-frac", type=float, default=0.5,
                    help="scene memory budget of the eviction measurement, as a fraction of the scenes' footprint")
@@ -90,14 +90,12 @@ def job_throughput(units_per_rank, world, ms_max):
     return world * units_per_rank / (ms_max / 1000.0)
 
 
-def bench_config(args, world, mean_visible=None):
-    """The `config` of both arms' lines."""
-    c = {"workload": WORKLOAD, "splats": args.splats, "width": args.width, "height": args.height, "sh_order": 3,
-         "depth_sorting": "Gpu", "blend": "unorm8", "poses": args.poses,
-         "l2": "inputs (1.4 GB scene) larger than L2", "parallelism": f"replicas x{world}"}
-    if mean_visible is not None:
-        c["mean_visible"] = int(mean_visible)
-    return c
+def bench_config(args, world):
+    """The `config` of both arms' lines: the workload only (the same scene, viewport and poses for
+    both); how each arm orders the splats is its line's `depth_sorting`."""
+    return {"workload": WORKLOAD, "splats": args.splats, "width": args.width, "height": args.height, "sh_order": 3,
+            "blend": "unorm8", "poses": args.poses,
+            "l2": "inputs (1.4 GB scene) larger than L2", "parallelism": f"replicas x{world}"}
 
 
 # ---------------------------------------------------------------------------------------------------
@@ -233,14 +231,14 @@ def load_peaks():
 
 
 # DRAM traffic per unit of the dominant kernel, from one ncu capture of a smaller case of the same
-# workload (profiles/k_raster_3m_1080p.md: 3M splats, 1920x1080, 3,353,969 pairs, 240.6 MB read + 6.4
+# workload (k_raster on 3M splats, 1920x1080, fly-through pose 2: 3,353,969 pairs, 240.6 MB read + 6.4
 # MB written): the reads grow with the pairs, the image write is per launch.  The bench scales it to
 # its own frames by their pair counts.
 TRAFFIC_PER_UNIT = {"raster": {"per_pair": 240.6e6 / 3353969.0, "per_launch": 6.4e6,
-                               "source": "profiles/k_raster_3m_1080p.md (3M-splat capture, scaled by pairs)"}}
+                               "source": "ncu capture of k_raster at 3M splats, 1080p (pose 2), scaled by pairs"}}
 # The raster is bound by instruction issue, not HBM: the fraction of issue slots its warps used in the
 # same capture (smsp__issue_active, pct of peak, active), reported beside the HBM figure.
-ISSUE_ACTIVE = {"raster": {"frac": 0.836, "source": "profiles/k_raster_3m_1080p.md smsp__issue_active"}}
+ISSUE_ACTIVE = {"raster": {"frac": 0.836, "source": "ncu smsp__issue_active of the same k_raster capture"}}
 
 
 def stage_traffic(stage, P):
@@ -463,7 +461,9 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered splats)",
-            "config": bench_config(args, world, vis_tot / frames_prof),
+            "config": bench_config(args, world),
+            "depth_sorting": "Gpu (composite depth key, shaders.wgsl:318-324; stable device radix sort)",
+            "mean_visible": int(vis_tot / frames_prof),
             "splats_per_s": round(value * args.splats, 0),
             "stages": stages, "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "cpu_baseline": cpu, "uhd": uhd, "graph": graph, "differentiation": diff, "loading": loading,
@@ -850,6 +850,7 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered splats)",
             "impl": "reference",
             "config": bench_config(args, world),
+            "depth_sorting": "Cpu (the reference's CPU depth-sort fallback, renderer.rs:372-395)",
             "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

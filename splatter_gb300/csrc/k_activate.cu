@@ -64,8 +64,8 @@ __global__ void __launch_bounds__(256) k_activate_backward(
 }
 
 static uint32_t grid_for(uint64_t n) {
-    uint64_t b = (n + 255) / 256;
-    return (uint32_t)(b < 152u * 16u ? (b ? b : 1) : 152u * 16u);
+    const uint64_t b = (n + 255) / 256, cap = (uint64_t)device_sm_count() * 16u;
+    return (uint32_t)(b < cap ? (b ? b : 1) : cap);
 }
 
 void launch_activate(uint32_t n, const float* means, const float* quats, const float* logs, const float* logits,

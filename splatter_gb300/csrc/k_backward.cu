@@ -316,7 +316,7 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
     const float psx = (2.0f * u.view_size[0]) / (float)W;
     const float psy = -((2.0f * u.view_size[1]) / (float)H);
     uint32_t zg = (max_n * GR + 255) / 256;
-    if (zg > 152u * 8u) zg = 152u * 8u;
+    if (zg > device_sm_count() * 8u) zg = device_sm_count() * 8u;
     if (zg == 0) zg = 1;
     k_zero_grad_rec<<<zg, 256, 0, st>>>(grad_rec, fc);
     const int grid = tiles_x * tiles_y;
@@ -330,7 +330,7 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
     }
     if (max_n == 0) return;
     uint32_t blocks = (max_n + 127) / 128;
-    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    if (blocks > device_sm_count() * 16u) blocks = device_sm_count() * 16u;
 #define PB(SHO, COV)                                                                                        \
     k_preprocess_backward<SHO, COV><<<blocks, 128, 0, st>>>(s, u, idx, fc, boxes, grad_rec, gx, gy, gz, grot,       \
                                                             gscale_alpha, gsh, accumulate)

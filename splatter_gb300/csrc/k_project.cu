@@ -306,7 +306,7 @@ void launch_preprocess(int sh_order, bool covariance, bool rect, const SceneView
                        cudaStream_t st) {
     if (max_n == 0) return;
     uint32_t blocks = (max_n + 255) / 256;
-    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    if (blocks > device_sm_count() * 16u) blocks = device_sm_count() * 16u;
     const dim3 g(blocks);
     switch (sh_order) {
         case 0: launch_pre1<0>(covariance, rect, g, s, u, idx, fc, rec, boxes, st); break;

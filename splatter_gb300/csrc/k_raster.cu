@@ -233,7 +233,7 @@ void launch_tile_ranges(const uint32_t* pair_keys, const FrameCounters* fc, uint
                         cudaStream_t st) {
     if (pair_cap == 0) return;
     uint32_t grid = (pair_cap + 255) / 256;
-    if (grid > 152u * 8u) grid = 152u * 8u;
+    if (grid > device_sm_count() * 8u) grid = device_sm_count() * 8u;
     k_tile_ranges<<<grid, 256, 0, st>>>(pair_keys, fc, pair_cap, ranges);
 }
 

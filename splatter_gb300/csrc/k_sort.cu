@@ -10,6 +10,8 @@
 //     frames) and bounded waits that raise an error bit instead of hanging;
 //   * dynamic tile ids and a persistent grid, so a wait only ever targets a tile held by a running CTA;
 //   * keys, then values, are scattered through shared memory so global writes are runs per digit.
+#include <atomic>
+
 #include "spl_device.cuh"
 
 namespace spl {
@@ -130,6 +132,18 @@ __global__ void __launch_bounds__(OS_THREADS, 3)
     }
 }
 
+uint32_t device_sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1u;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 1;
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return (uint32_t)v;
+}
+
 struct OnesweepShape {
     int num_sms = 1, blocks_per_sm = 1;
 };
@@ -192,7 +206,7 @@ void launch_histogram(const uint32_t* keys, const uint32_t* n_ptr, uint32_t n_ca
                       cudaStream_t st) {
     if (n_cap == 0) return;
     uint32_t grid = (n_cap + 255) / 256;
-    if (grid > 152u * 4u) grid = 152u * 4u;
+    if (grid > device_sm_count() * 4u) grid = device_sm_count() * 4u;
     k_histogram<<<grid, 256, 0, st>>>(keys, n_ptr, n_cap, hist4x256);
 }
 

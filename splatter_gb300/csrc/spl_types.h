@@ -69,6 +69,9 @@ struct SceneView {
 };
 
 // ---- launchers (defined in the .cu files) --------------------------------------------------------
+// Streaming multiprocessors of the current device (queried once per device, then cached); grids of
+// grid-stride kernels are capped at a multiple of it.
+uint32_t device_sm_count();
 void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st);  // counters + epoch only
 void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, const Uniforms& u, Uniforms* d_u, const SceneView& sv,
                         SceneView* d_sv, cudaStream_t st);

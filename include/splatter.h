@@ -110,6 +110,15 @@ SPL_API int spl_renderer_reserve(spl_renderer* r, uint32_t width, uint32_t heigh
 SPL_API int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
                      uint32_t height, void* out_device, void* stream);
 
+/* Frame graphs inside render_frame (extension, on by default): when two frames in a row on a renderer
+ * have the same viewport and scene size, the renderer captures the frame into a CUDA graph (grids
+ * sized for that scene, as the direct launches) and replays it for later frames of that viewport and
+ * size, any camera, any scene of that size and any output buffer — one graph launch instead of one
+ * launch per kernel, the same results.  Frames are launched directly while profiling is on, while
+ * the stream is being captured, and for other viewports and sizes.  enable = 0 turns it off (and
+ * frees the graph). */
+SPL_API int spl_renderer_set_frame_graphs(spl_renderer* r, int enable);
+
 /* ---- camera motors (renderer.rs:355-366, utils.rs:31-42) -------------------------------------------
  * The reference's render_frame takes a projective-geometric-algebra motor.  Layout here (the crate
  * geometric_algebra 0.3.0 that defines the reference's is not available; built from the algebra
@@ -326,7 +335,9 @@ SPL_API int spl_renderer_set_sort_mode(spl_renderer* r, int mode);
  * any such scene and any camera (only the first kernel's parameters change: the kernels read the
  * scene and every count from device memory), on any stream.  The renderer's scratch is shared with
  * its other frames: one frame of a renderer in flight at a time.  Destroy the graph before the
- * renderer or the output buffer. */
+ * renderer or the output buffer.  A later frame at a larger viewport reallocates the renderer's
+ * per-viewport scratch; a graph captured before that refuses to launch (SPL_ERR_INVALID): capture
+ * it again, or reserve the largest viewport first (spl_renderer_reserve). */
 typedef struct spl_frame_graph spl_frame_graph;
 SPL_API int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, uint64_t max_splats,
                                    void* out_device, spl_frame_graph** out);

@@ -138,6 +138,7 @@ SIGNATURES = [
     ("spl_renderer_set_profiling", I32, [P, I32]),
     ("spl_renderer_stage_times", I32, [P, ctypes.POINTER(ctypes.c_float), I32]),
     ("spl_renderer_launches_per_frame", I32, [P, U32, U32]),
+    ("spl_renderer_set_frame_graphs", I32, [P, I32]),
     ("spl_sort_pairs_no_alloc", I32, [P, P, P, P, U64, U32, P]),
     ("spl_sort_pairs_no_alloc_status", I32, [P, P]),
     ("spl_scene_wrap", I32, [P, U64, P, P, P, P, P, P, ctypes.POINTER(P)]),

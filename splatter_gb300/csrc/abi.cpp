@@ -104,10 +104,17 @@ static int validate_config(const spl_config* c) {
     return SPL_OK;
 }
 
+extern "C" {
+static void drop_own_graph(spl_renderer* r);  // defined with the frame graphs (C linkage there)
+}
+
 static int ensure_ranges(spl_renderer* r, uint64_t tiles) {
     if (tiles <= r->ranges_cap) return SPL_OK;
     cudaError_t e = cudaDeviceSynchronize();  // the old buffer may still be read by a frame in flight
     if (e != cudaSuccess) return fail(SPL_ERR_CUDA, "ranges resize: %s", cudaGetErrorString(e));
+    // frame graphs captured with the old buffers must not run again
+    drop_own_graph(r);
+    ++r->scratch_generation;
     dfree(r->ranges);
     dfree(r->tile_order);
     r->ranges_cap = 0;
@@ -289,6 +296,7 @@ int spl_renderer_create(const spl_config* cfg, spl_renderer** out) {
 void spl_renderer_destroy(spl_renderer* r) {
     if (!r) return;
     cudaDeviceSynchronize();
+    drop_own_graph(r);
     r->release();
     delete r;
 }
@@ -396,6 +404,10 @@ int spl_render_frame_motor(spl_renderer* r, const spl_scene* scene, const float 
     return spl_render_frame(r, scene, cam, width, height, out_device, stream);
 }
 
+static int frame_graph_replay(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16],
+                              void* out_device, cudaStream_t st);
+static bool own_graph_matches(const spl_renderer* r, uint32_t w, uint32_t h, uint64_t n);
+
 int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera_to_world[16], uint32_t width,
                      uint32_t height, void* out_device, void* stream) {
     if (!r || !scene || !camera_to_world || !out_device) return fail(SPL_ERR_INVALID, "NULL argument");
@@ -403,10 +415,31 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
         return fail(SPL_ERR_INVALID, "viewport %ux%u outside [1, 65535]", width, height);
     if (scene->n > r->max_n) return fail(SPL_ERR_INVALID, "scene larger than the renderer's max_splat_count");
     cudaStream_t st = (cudaStream_t)stream;
+    // The second frame in a row of the same viewport and scene size is captured into a frame graph
+    // (grids sized for the scene, exactly as the direct launches), and frames of that key replay it:
+    // one graph launch instead of a launch per kernel.  Not while profiling (the stage events are
+    // direct launches) or while the caller's stream is being captured.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const bool capturing = cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+    if (r->frame_graphs && !r->profiling && !capturing && scene->n > 0) {
+        if (!own_graph_matches(r, width, height, scene->n) && r->seen_w == width && r->seen_h == height &&
+            r->seen_n == scene->n) {
+            drop_own_graph(r);
+            spl_frame_graph* g = nullptr;
+            const int rc = spl_frame_graph_create(r, width, height, scene->n, out_device, &g);
+            if (rc) return rc;
+            r->own_graph = g;
+        }
+        if (own_graph_matches(r, width, height, scene->n))
+            return frame_graph_replay(r->own_graph, scene, camera_to_world, out_device, st);
+    }
     Uniforms u;
     compute_uniforms(r->cfg, camera_to_world, width, height, u);
     const int rc = render_frame_impl(r, scene->view(), u, width, height, out_device, st, (uint32_t)scene->n);
     if (rc) return rc;
+    r->seen_w = width;
+    r->seen_h = height;
+    r->seen_n = scene->n;
     r->last_stream = st;
     r->last_scene = scene;
     r->last_u = u;
@@ -414,6 +447,13 @@ int spl_render_frame(spl_renderer* r, const spl_scene* scene, const float camera
     r->last_w = width;
     r->last_h = height;
     r->last_n = scene->n;
+    return SPL_OK;
+}
+
+int spl_renderer_set_frame_graphs(spl_renderer* r, int enable) {
+    if (!r) return fail(SPL_ERR_INVALID, "NULL argument");
+    r->frame_graphs = enable != 0;
+    if (!r->frame_graphs) drop_own_graph(r);
     return SPL_OK;
 }
 
@@ -435,6 +475,7 @@ int spl_renderer_set_sort_mode(spl_renderer* r, int mode) {
         CU(cudaDeviceSynchronize());
         onesweep_prepare();
     }
+    if (mode != r->sort_mode) drop_own_graph(r);  // its sorts are the other algorithm's
     r->sort_mode = mode;
     return SPL_OK;
 }
@@ -874,12 +915,26 @@ struct spl_frame_graph {
     spl_renderer* r = nullptr;
     uint32_t w = 0, h = 0;
     uint64_t max_splats = 0;  // the grids' bound
+    uint32_t generation = 0;  // the renderer's scratch generation the graph was captured with
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t begin_node = nullptr;  // k_frame_begin: the node whose parameters carry camera and scene
     cudaKernelNodeParams begin_params{};
+    cudaGraphNode_t raster_node = nullptr;  // the raster: its output pointer can be re-targeted
+    cudaKernelNodeParams raster_params{};
+    void* out = nullptr;  // the output the raster node writes now
     const uint32_t* final_pair_vals = nullptr;
 };
+
+static void drop_own_graph(spl_renderer* r) {
+    if (r->own_graph) spl_frame_graph_destroy(r->own_graph);  // an exec in flight is freed when it completes
+    r->own_graph = nullptr;
+}
+
+static bool own_graph_matches(const spl_renderer* r, uint32_t w, uint32_t h, uint64_t n) {
+    const spl_frame_graph* g = r->own_graph;
+    return g && g->w == w && g->h == h && g->max_splats == n && g->generation == r->scratch_generation;
+}
 
 void spl_frame_graph_destroy(spl_frame_graph* g) {
     if (!g) return;
@@ -904,6 +959,8 @@ int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, uin
     g->w = width;
     g->h = height;
     g->max_splats = max_splats;
+    g->generation = r->scratch_generation;
+    g->out = out_device;
     cudaStream_t cs = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -932,17 +989,23 @@ int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, uin
         e = cudaGraphGetNodes(g->graph, nullptr, &nn);
         std::vector<cudaGraphNode_t> nodes(nn);
         if (e == cudaSuccess && nn) e = cudaGraphGetNodes(g->graph, nodes.data(), &nn);
-        for (size_t i = 0; e == cudaSuccess && i < nn && !g->begin_node; ++i) {
+        const void* raster = raster_kernel(r->cfg.use_unaligned_rectangles != 0, r->cfg.blend_mode);
+        for (size_t i = 0; e == cudaSuccess && i < nn; ++i) {
             cudaGraphNodeType t;
             if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
             cudaKernelNodeParams kp{};
-            if (cudaGraphKernelNodeGetParams(nodes[i], &kp) == cudaSuccess && kp.func == frame_begin_kernel()) {
+            if (cudaGraphKernelNodeGetParams(nodes[i], &kp) != cudaSuccess) continue;
+            if (kp.func == frame_begin_kernel()) {
                 g->begin_node = nodes[i];
                 g->begin_params = kp;
+            } else if (kp.func == raster) {
+                g->raster_node = nodes[i];
+                g->raster_params = kp;
             }
         }
         if (e != cudaSuccess) rc = fail(SPL_ERR_CUDA, "cudaGraphGetNodes: %s", cudaGetErrorString(e));
         else if (!g->begin_node) rc = fail(SPL_ERR_CUDA, "captured frame has no frame-begin node");
+        else if (!g->raster_node) rc = fail(SPL_ERR_CUDA, "captured frame has no raster node");
     }
     if (!rc) {
         e = cudaGraphInstantiate(&g->exec, g->graph, 0);
@@ -957,12 +1020,13 @@ int spl_frame_graph_create(spl_renderer* r, uint32_t width, uint32_t height, uin
     return SPL_OK;
 }
 
-int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16], void* stream) {
-    if (!g || !scene || !camera_to_world) return fail(SPL_ERR_INVALID, "NULL argument");
+// One replay of a captured frame: the first node takes the camera and the scene, the raster node
+// the output when it differs from the one it writes now.
+static int frame_graph_replay(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16],
+                              void* out_device, cudaStream_t st) {
     spl_renderer* r = g->r;
-    if (scene->n > g->max_splats)
-        return fail(SPL_ERR_INVALID, "scene of %llu splats exceeds the graph's bound %llu",
-                    (unsigned long long)scene->n, (unsigned long long)g->max_splats);
+    if (g->generation != r->scratch_generation)
+        return fail(SPL_ERR_INVALID, "the renderer's viewport scratch was reallocated (a larger frame): recreate the graph");
     Uniforms u;
     compute_uniforms(r->cfg, camera_to_world, g->w, g->h, u);
     SceneView sv = scene->view();
@@ -975,8 +1039,20 @@ int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const flo
     kp.kernelParams = args;
     kp.extra = nullptr;
     CU(cudaGraphExecKernelNodeSetParams(g->exec, g->begin_node, &kp));
-    CU(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
-    r->last_stream = (cudaStream_t)stream;
+    if (out_device != g->out) {
+        // the other arguments keep their captured values (the graph node holds them)
+        void* rargs[RASTER_OUT_ARG + 1];
+        for (int i = 0; i < RASTER_OUT_ARG; ++i) rargs[i] = g->raster_params.kernelParams[i];
+        void* out = out_device;
+        rargs[RASTER_OUT_ARG] = &out;
+        cudaKernelNodeParams rp = g->raster_params;
+        rp.kernelParams = rargs;
+        rp.extra = nullptr;
+        CU(cudaGraphExecKernelNodeSetParams(g->exec, g->raster_node, &rp));
+        g->out = out_device;
+    }
+    CU(cudaGraphLaunch(g->exec, st));
+    r->last_stream = st;
     r->last_scene = scene;
     r->last_u = u;
     r->has_frame = true;
@@ -985,6 +1061,14 @@ int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const flo
     r->last_n = scene->n;
     r->final_pair_vals = g->final_pair_vals;
     return SPL_OK;
+}
+
+int spl_frame_graph_launch(spl_frame_graph* g, const spl_scene* scene, const float camera_to_world[16], void* stream) {
+    if (!g || !scene || !camera_to_world) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (scene->n > g->max_splats)
+        return fail(SPL_ERR_INVALID, "scene of %llu splats exceeds the graph's bound %llu",
+                    (unsigned long long)scene->n, (unsigned long long)g->max_splats);
+    return frame_graph_replay(g, scene, camera_to_world, g->out, (cudaStream_t)stream);
 }
 
 int spl_scene_load_chunk_device(spl_scene* s, const float* records_device, uint64_t start, uint64_t count,

@@ -527,6 +527,13 @@ __global__ void __launch_bounds__(256, 6) k_raster(const uint2* __restrict__ ran
     }
 }
 
+const void* raster_kernel(bool rect, int blend) {
+    if (rect) return blend == 0 ? reinterpret_cast<const void*>(&k_raster<true, 0>)
+                                : reinterpret_cast<const void*>(&k_raster<true, 1>);
+    return blend == 0 ? reinterpret_cast<const void*>(&k_raster<false, 0>)
+                      : reinterpret_cast<const void*>(&k_raster<false, 1>);
+}
+
 void launch_raster(bool rect, int blend, const uint2* ranges, uint32_t* tile_order, const uint32_t* pair_vals,
                    const float4* rec, const Uniforms& u, void* out, cudaStream_t st) {
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];

@@ -426,6 +426,9 @@ int spl_server_create(const spl_config* cfg, const spl_server_config* scfg, spl_
         if (!rc && scfg->slots > 1) rc = spl_renderer_set_sort_mode(slot->r, SPL_SORT_ONESWEEP);
         // concurrent frames already fill the device at a frame's end: the tile order would only add work
         if (!rc && scfg->slots > 1) slot->r->order_tiles = false;
+        // the slots capture their own graphs per viewport and size class (use_graphs); otherwise frames
+        // are launched directly, whatever the order of scenes
+        if (!rc) slot->r->frame_graphs = false;
         if (!rc) rc = spl_renderer_reserve(slot->r, scfg->max_width, scfg->max_height);
         if (!rc) {
             e = cudaStreamCreateWithFlags(&slot->st, cudaStreamNonBlocking);

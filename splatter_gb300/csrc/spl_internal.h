@@ -66,6 +66,8 @@ void compute_uniforms(const spl_config& cfg, const float* cam, uint32_t W, uint3
 
 using namespace spl;  // the structs below use the device-side types
 
+struct spl_frame_graph;
+
 struct spl_renderer {
     spl_config cfg{};
     int device = 0;
@@ -92,7 +94,13 @@ struct spl_renderer {
     uint2* ranges = nullptr;
     uint32_t* tile_order = nullptr;  // the raster's tile order, most pairs first (ranges_cap entries)
     bool order_tiles = true;         // off where concurrent frames already hide the raster's tail (serving)
+    // render_frame replays a frame graph it captured itself once a viewport and scene size repeat
+    bool frame_graphs = true;
+    spl_frame_graph* own_graph = nullptr;  // the captured frame of (own_w, own_h, own_n)
+    uint32_t seen_w = 0, seen_h = 0;       // the previous direct frame's key
+    uint64_t seen_n = 0;
     uint64_t ranges_cap = 0;
+    uint32_t scratch_generation = 0;  // bumped when the per-viewport scratch is reallocated (graphs hold it)
     // last frame
     cudaStream_t last_stream = nullptr;
     bool has_frame = false;

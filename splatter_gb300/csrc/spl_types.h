@@ -76,6 +76,8 @@ void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, cudaStream_t st
 void launch_frame_begin(FrameCounters* fc, uint32_t* epoch_word, const Uniforms& u, Uniforms* d_u, const SceneView& sv,
                         SceneView* d_sv, cudaStream_t st);
 const void* frame_begin_kernel();  // host handle of k_frame_begin (to find its node in a captured graph)
+const void* raster_kernel(bool rect, int blend);  // host handle of the raster kernel (its output is re-targeted)
+constexpr int RASTER_OUT_ARG = 10;                // index of the raster kernel's output-pointer argument
 // grid_n: the splat count the grid is sized for (the scene's, or the renderer's maximum for a
 // captured frame whose scene changes between launches); the kernels read the scene from d_sv.
 // hist: also build the digit histograms of the keys (the onesweep passes need them).

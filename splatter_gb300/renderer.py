@@ -197,6 +197,11 @@ class Renderer:
     def set_profiling(self, enable=True):
         check(self._lib.spl_renderer_set_profiling(self._h, 1 if enable else 0))
 
+    def set_frame_graphs(self, enable=True):
+        """Replay frames of a repeated viewport and scene size from a graph the renderer captures
+        itself (on by default; the same results as direct launches)."""
+        check(self._lib.spl_renderer_set_frame_graphs(self._h, 1 if enable else 0))
+
     def set_sort_mode(self, mode):
         """SORT_COOPERATIVE (default, one frame on the device at a time) or SORT_ONESWEEP (safe with
         frames of other renderers running concurrently)."""

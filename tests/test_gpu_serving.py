@@ -66,6 +66,38 @@ def test_frame_graph_and_onesweep_match_direct(cuda):
     gs.close()
 
 
+def test_render_frame_replays_its_own_graph(cuda):
+    """render_frame captures the second frame in a row of a viewport and scene size into a graph and
+    replays it for the frames that follow: every frame equals a direct launch bit for bit, with the
+    output buffer alternating, another scene of the same size, a larger viewport in between (which
+    reallocates the per-viewport scratch) and the viewport changing back; the frame state (counters,
+    entries) follows the replayed frame."""
+    import torch
+    n = 60000
+    recs = [synthetic.clustered(n, seed=3, sh_order=3), synthetic.clustered(n, seed=5, sh_order=3)]
+    poses = camera.orbit_poses(10, seed=6, radius=(6.0, 14.0))
+    direct = Renderer(_cfg(n))
+    direct.set_frame_graphs(False)
+    r = Renderer(_cfg(n))
+    sd = [_scene_on(direct, x) for x in recs]
+    sr = [_scene_on(r, x) for x in recs]
+    bufs = {vp: [r.output_buffer(*vp) for _ in range(2)] for vp in ((320, 240), (640, 360))}
+    plan = [(0, (320, 240)), (0, (320, 240)), (0, (320, 240)), (1, (320, 240)), (0, (640, 360)),
+            (1, (640, 360)), (1, (640, 360)), (0, (320, 240)), (0, (320, 240)), (1, (320, 240))]
+    for k, (si, vp) in enumerate(plan):
+        want = direct.render_frame(sd[si], poses[k], *vp).cpu()
+        got = r.render_frame(sr[si], poses[k], *vp, out=bufs[vp][k % 2])
+        torch.cuda.synchronize()
+        assert torch.equal(got.cpu(), want), f"frame {k}"
+        a, b = r.frame_info(), direct.frame_info()
+        assert (a.visible_count, a.draw_count, a.pair_count, a.width, a.height) == \
+            (b.visible_count, b.draw_count, b.pair_count, b.width, b.height)
+        ka, ia, _ = r.sorted_entries()
+        kb, ib, _ = direct.sorted_entries()
+        assert torch.equal(ka, kb) and torch.equal(ia, ib)
+    assert int((want[..., 3] != 255).sum()) > 1000  # something drawn
+
+
 def _scene_on(renderer, rec):
     sc = Scene(renderer, rec.shape[0])
     sc.load_chunk(rec)

@@ -53,6 +53,8 @@ def parse_args(argv=None):
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-differentiation", action="store_true", help="skip the forward+backward leg")
+    p.add_argument("--only-differentiation", action="store_true",
+                   help="run only the forward+backward leg and print its JSON object (for launch lists)")
     p.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain leg")
     p.add_argument("--no-uhd", action="store_true", help="skip the 3840x2160 measurement")
     p.add_argument("--no-loading", action="store_true", help="skip the splat-file loading leg")
@@ -534,13 +536,13 @@ def run_loading(args, n=1_000_000, chunk=32768, W=1920, H=1080):
             "progressive_result_equals_whole_load": same}
 
 
-def run_differentiation(args, iters=5, warmup=3):
+def run_differentiation(args, iters=5, warmup=3, full=True):
     """Forward+backward ms/iter through torch.autograd (the loader's activations and the hand-written
     backward behind autograd Functions).  One iteration = the 8 views rendered, compared with their
     targets and back-propagated, gradients summed over the views: `ms_per_iter` with the 8 views in
     one node (render_raw_views: one renderer per view, gradients added in place on the GPU),
     `ms_per_iter_view_nodes` with one render_raw node and one backward call per view (autograd sums
-    the per-view gradient arrays)."""
+    the per-view gradient arrays).  full=False times the one-node iteration alone."""
     import numpy as np
     import torch
     from splatter_gb300 import BlendMode, Configuration, Renderer, camera, synthetic
@@ -605,8 +607,12 @@ def run_differentiation(args, iters=5, warmup=3):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / iters, out
 
-    ms_nodes, loss_nodes = timed(iteration)
+    ms_nodes, loss_nodes = timed(iteration) if full else (None, None)
     ms, loss = timed(iteration_views)
+    finite = all(bool(torch.isfinite(t.grad).all()) for t in leaves)
+    if not full:
+        return {"workload": DIFF_WORKLOAD, "ms_per_iter": round(ms, 3), "views": views, "splats": n,
+                "iters": iters, "warmup": warmup, "loss": float(loss), "grads_finite": finite}
     # forward alone (no graph), same views
     with torch.no_grad():
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -617,7 +623,6 @@ def run_differentiation(args, iters=5, warmup=3):
         f1.record(stream)
         torch.cuda.synchronize()
     ms_fwd = f0.elapsed_time(f1) / iters
-    finite = all(bool(torch.isfinite(t.grad).all()) for t in leaves)
     return {"workload": DIFF_WORKLOAD, "ms_per_iter": round(ms, 3), "ms_forward_per_iter": round(ms_fwd, 3),
             "ms_per_iter_view_nodes": round(ms_nodes, 3), "loss_view_nodes": float(loss_nodes),
             "views": views, "splats": n, "iters": iters, "warmup": warmup, "loss": float(loss),
@@ -867,6 +872,8 @@ def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_differentiation:
+        print(json.dumps(run_differentiation(args, full=False)), flush=True)
     else:
         run_ours(args)
 

@@ -529,14 +529,18 @@ static int render_backward(spl_renderer* r, const spl_scene* scene, const float*
         return fail(SPL_ERR_INVALID, "render this scene with spl_render_frame first (the backward reuses that frame)");
     if (!r->grad_rec) {
         int rc = dalloc(&r->grad_rec, r->max_n * 10);
-        if (rc) return rc;
+        if (!rc) rc = dalloc(&r->grad_deferred, r->max_n + 1);
+        if (rc) {
+            dfree(r->grad_rec);
+            return rc;
+        }
     }
     cudaStream_t st = (cudaStream_t)stream;
     const spl_config& cfg = r->cfg;
     launch_backward((int)cfg.spherical_harmonics_order, cfg.use_covariance_for_scale != 0,
                     cfg.use_unaligned_rectangles != 0, scene->view(), r->last_u, r->idx, r->fc, r->boxes, r->ranges,
                     r->order_tiles ? r->tile_order : nullptr, r->final_pair_vals, r->rec, reinterpret_cast<const float4*>(image_device),
-                    reinterpret_cast<const float4*>(grad_image_device), r->grad_rec, (uint32_t)scene->n, grad_x,
+                    reinterpret_cast<const float4*>(grad_image_device), r->grad_rec, r->grad_deferred, (uint32_t)scene->n, grad_x,
                     grad_y, grad_z, reinterpret_cast<float4*>(grad_rotation), reinterpret_cast<float4*>(grad_scale_alpha),
                     grad_sh, accumulate, st);
     CU(cudaGetLastError());

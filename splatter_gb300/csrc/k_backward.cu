@@ -14,19 +14,21 @@
 // and the chain through sat(), the falloff and tc = A (X, Y) + B gives per-splat gradients of the
 // record (A00, A01, B0, A10, A11, B1, a, r, g, b), reduced over each 8-lane pixel group before one
 // set of global float atomics per (splat, group).  A is accumulated against pixel offsets from the
-// centre of the splat's pixel box and B at that centre (well conditioned; see vertex_math).
+// centre of the splat's pixel box and B at that centre (well conditioned; see vertex_vjp_t).
 //
 // k_preprocess_backward maps those record gradients to the splat parameters (centre, rotation,
-// scale, opacity, SH): the vertex stage runs on forward-mode dual numbers once per input direction
-// (centre x/y/z, quaternion 4, scale 3), so the Jacobian is exactly that of the forward arithmetic;
-// SH coefficient gradients are the basis values times the colour gradients.
+// scale, opacity, SH) in reverse mode (vertex_vjp_t): one sweep of the vertex stage's values, one
+// sweep of adjoints back through the same formulas, in float; needles and discs (needs_double_sweep)
+// are left to k_preprocess_backward_double, which sweeps them in double.  SH coefficient gradients
+// are the basis values times the colour gradients.
 #include "spl_vertex.cuh"
 
 namespace spl {
 
 constexpr int GR = 10;  // gradient words per record
 
-__global__ void k_zero_grad_rec(float* grad_rec, const FrameCounters* fc) {
+__global__ void k_zero_grad_rec(float* grad_rec, const FrameCounters* fc, uint32_t* deferred) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) deferred[0] = 0u;
     const uint32_t n = fc->visible * GR;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) grad_rec[i] = 0.0f;
 }
@@ -201,87 +203,89 @@ __global__ void __launch_bounds__(256) k_raster_backward(const uint2* __restrict
     }
 }
 
+// One splat's inputs to the vertex-stage backward: its parameters and SH coefficients, and the view-plane
+// position of its record's reference pixel (the centre of the record's pixel box).
+template <int SHO>
+struct VjpInputs {
+    float cx, cy, cz, rx, ry;
+    float4 rot, sca;
+    float sh[48];
+    __device__ __forceinline__ void load(const SceneView& s, const Uniforms& u, uint32_t i, uint2 bb) {
+        cx = __ldg(s.x + i);
+        cy = __ldg(s.y + i);
+        cz = __ldg(s.z + i);
+        rot = __ldg(s.rot + i);
+        sca = __ldg(s.scale_alpha + i);
+        constexpr int NF = 3 * (SHO + 1) * (SHO + 1);
+        const float* p = s.sh + (size_t)i * 48;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) sh[k] = __ldg(p + k);
+        const float Xr = 0.5f * (float)((bb.x & 0xFFFFu) + (bb.y & 0xFFFFu) + 1u);
+        const float Yr = 0.5f * (float)((bb.x >> 16) + (bb.y >> 16) + 1u);
+        const float vw = u.view_size[0], vh = u.view_size[1];
+        rx = Xr * ((2.0f * vw) / (float)u.image_size[0]) - vw;
+        ry = vh - Yr * ((2.0f * vh) / (float)u.image_size[1]);
+    }
+};
+
+__device__ __forceinline__ bool load_record_gradient(const float* grad_rec, uint32_t slot, float* g) {
+    const float* gr = grad_rec + (size_t)slot * GR;
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < GR; ++k) {
+        g[k] = gr[k];
+        any = any || g[k] != 0.0f;
+    }
+    return any;  // false: not drawn, or no gradient reached it
+}
+
+// The centre, rotation, scale and opacity gradients of splat i (set, or added to what is there).
+__device__ __forceinline__ void store_splat_gradient(uint32_t i, const float* gin, float galpha, float* gx, float* gy,
+                                                     float* gz, float4* grot, float4* gscale_alpha, bool accumulate) {
+    if (accumulate) {  // several frames' gradients summed in place, one frame after another
+        const float4 r0 = grot[i], s0 = gscale_alpha[i];
+        gx[i] += gin[0];
+        gy[i] += gin[1];
+        gz[i] += gin[2];
+        grot[i] = make_float4(r0.x + gin[3], r0.y + gin[4], r0.z + gin[5], r0.w + gin[6]);
+        gscale_alpha[i] = make_float4(s0.x + gin[7], s0.y + gin[8], s0.z + gin[9], s0.w + galpha);
+    } else {
+        gx[i] = gin[0];
+        gy[i] = gin[1];
+        gz[i] = gin[2];
+        grot[i] = make_float4(gin[3], gin[4], gin[5], gin[6]);
+        gscale_alpha[i] = make_float4(gin[7], gin[8], gin[9], galpha);
+    }
+}
+
+// Float sweep of every drawn splat but the needles and discs (needs_double_sweep), whose slots go to
+// `deferred` ([0] the count, then the slots) for k_preprocess_backward_double; SH gradients of all.
 template <int SHO, bool COV>
-__global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
+__global__ void __launch_bounds__(128, 3) k_preprocess_backward(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
                                                              const FrameCounters* __restrict__ fc,
                                                              const uint2* __restrict__ boxes,
                                                              const float* __restrict__ grad_rec, float* gx, float* gy,
                                                              float* gz, float4* grot, float4* gscale_alpha,
-                                                             float* gsh, bool accumulate) {
+                                                             float* gsh, uint32_t* deferred, uint32_t deferred_cap,
+                                                             bool accumulate) {
     const uint32_t V = fc->visible;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < V; slot += gridDim.x * blockDim.x) {
-        const float* gr = grad_rec + (size_t)slot * GR;
         float g[GR];
-        bool any = false;
-#pragma unroll
-        for (int k = 0; k < GR; ++k) {
-            g[k] = gr[k];
-            any = any || g[k] != 0.0f;
-        }
-        if (!any) continue;  // not drawn, or no gradient reached it
+        if (!load_record_gradient(grad_rec, slot, g)) continue;
         const uint32_t i = __ldg(idx + slot);
-        const float cx = __ldg(s.x + i), cy = __ldg(s.y + i), cz = __ldg(s.z + i);
-        const float4 rot = __ldg(s.rot + i);
-        const float4 sca = __ldg(s.scale_alpha + i);
-        float sh[48];
-        {
-            constexpr int NF = 3 * (SHO + 1) * (SHO + 1);
-            const float* p = s.sh + (size_t)i * 48;
-#pragma unroll
-            for (int k = 0; k < NF; ++k) sh[k] = __ldg(p + k);
-        }
-        const float in[10] = {cx, cy, cz, rot.x, rot.y, rot.z, rot.w, sca.x, sca.y, sca.z};
-        // reference pixel: the centre of the record's pixel box, as a view-plane position
-        const uint2 bb = __ldg(boxes + slot);
-        const float Xr = 0.5f * (float)((bb.x & 0xFFFFu) + (bb.y & 0xFFFFu) + 1u);
-        const float Yr = 0.5f * (float)((bb.x >> 16) + (bb.y >> 16) + 1u);
-        const float vw = u.view_size[0], vh = u.view_size[1];
-        const float rx = Xr * ((2.0f * vw) / (float)u.image_size[0]) - vw;
-        const float ry = vh - Yr * ((2.0f * vh) / (float)u.image_size[1]);
-        float gin[10];
-        // centre directions: geometry and colour (the view direction moves with the centre)
-#pragma unroll 1
-        for (int dir = 0; dir < 3; ++dir) {
-            Df d[10];
-#pragma unroll
-            for (int k = 0; k < 10; ++k) d[k] = Df{in[k], k == dir ? 1.0f : 0.0f};
-            VertexOut<Df> o;
-            vertex_math<SHO, COV, Df, true>(u, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], sh, o, rx,
-                                            ry);
-            float acc = (g[0] * o.A00.d + g[1] * o.A01.d) + (g[2] * o.B0r.d + g[3] * o.A10.d);
-            acc += (g[4] * o.A11.d + g[5] * o.B1r.d);
-            acc += (g[7] * o.cr.d + g[8] * o.cg.d) + g[9] * o.cb.d;
-            gin[dir] = isfinite(acc) ? acc : 0.0f;
-        }
-        // rotation and scale directions: the colour does not depend on them
-#pragma unroll 1
-        for (int dir = 3; dir < 10; ++dir) {
-            Df d[10];
-#pragma unroll
-            for (int k = 0; k < 10; ++k) d[k] = Df{in[k], k == dir ? 1.0f : 0.0f};
-            VertexOut<Df> o;
-            vertex_math<SHO, COV, Df, true, false>(u, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9], sh,
-                                                   o, rx, ry);
-            float acc = (g[0] * o.A00.d + g[1] * o.A01.d) + (g[2] * o.B0r.d + g[3] * o.A10.d);
-            acc += (g[4] * o.A11.d + g[5] * o.B1r.d);
-            gin[dir] = isfinite(acc) ? acc : 0.0f;
-        }
-        if (accumulate) {  // several frames' gradients summed in place, one frame after another
-            const float4 r0 = grot[i], s0 = gscale_alpha[i];
-            gx[i] += gin[0];
-            gy[i] += gin[1];
-            gz[i] += gin[2];
-            grot[i] = make_float4(r0.x + gin[3], r0.y + gin[4], r0.z + gin[5], r0.w + gin[6]);
-            gscale_alpha[i] = make_float4(s0.x + gin[7], s0.y + gin[8], s0.z + gin[9], s0.w + g[6]);
+        VjpInputs<SHO> in;
+        in.load(s, u, i, __ldg(boxes + slot));
+        if (needs_double_sweep(in.sca.x, in.sca.y, in.sca.z)) {
+            const uint32_t pos = atomicAdd(deferred, 1u);
+            if (pos < deferred_cap) deferred[1 + pos] = slot;
         } else {
-            gx[i] = gin[0];
-            gy[i] = gin[1];
-            gz[i] = gin[2];
-            grot[i] = make_float4(gin[3], gin[4], gin[5], gin[6]);
-            gscale_alpha[i] = make_float4(gin[7], gin[8], gin[9], g[6]);
+            float gin[10];
+            vertex_vjp_t<float, SHO, COV>(u, in.cx, in.cy, in.cz, in.rot.x, in.rot.y, in.rot.z, in.rot.w, in.sca.x,
+                                          in.sca.y, in.sca.z, in.sh, in.rx, in.ry, g, gin);
+            store_splat_gradient(i, gin, g[6], gx, gy, gz, grot, gscale_alpha, accumulate);
         }
         // SH: rgb_c = 0.5 + sum_k B_k(d) sh[3k + c]
-        const float vx = cx - u.camera[12], vy = cy - u.camera[13], vz = cz - u.camera[14];
+        const float vx = in.cx - u.camera[12], vy = in.cy - u.camera[13], vz = in.cz - u.camera[14];
         const float len = sqrtf((vx * vx + vy * vy) + vz * vz);
         float B[16];
         sh_basis<SHO>(vx / len, vy / len, vz / len, B);
@@ -305,10 +309,35 @@ __global__ void __launch_bounds__(128) k_preprocess_backward(SceneView s, Unifor
     }
 }
 
+// The deferred needles and discs, swept in double (same formulas, same float forward values).
+template <int SHO, bool COV>
+__global__ void __launch_bounds__(128) k_preprocess_backward_double(SceneView s, Uniforms u,
+                                                                    const uint32_t* __restrict__ idx,
+                                                                    const uint2* __restrict__ boxes,
+                                                                    const float* __restrict__ grad_rec, float* gx,
+                                                                    float* gy, float* gz, float4* grot,
+                                                                    float4* gscale_alpha,
+                                                                    const uint32_t* __restrict__ deferred,
+                                                                    uint32_t deferred_cap, bool accumulate) {
+    const uint32_t n = min(deferred[0], deferred_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t slot = deferred[1 + k];
+        float g[GR];
+        load_record_gradient(grad_rec, slot, g);
+        const uint32_t i = __ldg(idx + slot);
+        VjpInputs<SHO> in;
+        in.load(s, u, i, __ldg(boxes + slot));
+        float gin[10];
+        vertex_vjp_t<double, SHO, COV>(u, in.cx, in.cy, in.cz, in.rot.x, in.rot.y, in.rot.z, in.rot.w, in.sca.x,
+                                       in.sca.y, in.sca.z, in.sh, in.rx, in.ry, g, gin);
+        store_splat_gradient(i, gin, g[6], gx, gy, gz, grot, gscale_alpha, accumulate);
+    }
+}
+
 void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
                      const uint32_t* idx, const FrameCounters* fc, const uint2* boxes, const uint2* ranges,
                      const uint32_t* tile_order, const uint32_t* pair_vals, const float4* rec, const float4* image,
-                     const float4* grad_image, float* grad_rec,
+                     const float4* grad_image, float* grad_rec, uint32_t* deferred,
                      uint32_t max_n, float* gx, float* gy, float* gz, float4* grot, float4* gscale_alpha, float* gsh,
                      bool accumulate, cudaStream_t st) {
     const int W = (int)u.image_size[0], H = (int)u.image_size[1];
@@ -318,7 +347,7 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
     uint32_t zg = (max_n * GR + 255) / 256;
     if (zg > device_sm_count() * 8u) zg = device_sm_count() * 8u;
     if (zg == 0) zg = 1;
-    k_zero_grad_rec<<<zg, 256, 0, st>>>(grad_rec, fc);
+    k_zero_grad_rec<<<zg, 256, 0, st>>>(grad_rec, fc, deferred);
     const int grid = tiles_x * tiles_y;
     if (grid > 0) {
         if (rect)
@@ -331,9 +360,16 @@ void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& 
     if (max_n == 0) return;
     uint32_t blocks = (max_n + 127) / 128;
     if (blocks > device_sm_count() * 16u) blocks = device_sm_count() * 16u;
-#define PB(SHO, COV)                                                                                        \
-    k_preprocess_backward<SHO, COV><<<blocks, 128, 0, st>>>(s, u, idx, fc, boxes, grad_rec, gx, gy, gz, grot,       \
-                                                            gscale_alpha, gsh, accumulate)
+    // the double sweep's grid: a few blocks per SM (needles and discs are few; the count is on the device)
+    const uint32_t dblocks = device_sm_count() * 2u;
+#define PB(SHO, COV)                                                                                          \
+    do {                                                                                                      \
+        k_preprocess_backward<SHO, COV><<<blocks, 128, 0, st>>>(s, u, idx, fc, boxes, grad_rec, gx, gy, gz, grot, \
+                                                                gscale_alpha, gsh, deferred, max_n, accumulate); \
+        k_preprocess_backward_double<SHO, COV><<<dblocks, 128, 0, st>>>(s, u, idx, boxes, grad_rec, gx, gy, gz,   \
+                                                                        grot, gscale_alpha, deferred, max_n,      \
+                                                                        accumulate);                              \
+    } while (0)
     switch (sh_order * 2 + (covariance ? 1 : 0)) {
         case 0: PB(0, false); break;
         case 1: PB(0, true); break;

@@ -110,6 +110,7 @@ struct spl_renderer {
     const spl_scene* last_scene = nullptr;
     Uniforms last_u{};
     float* grad_rec = nullptr;  // [max_n][10] record gradients of the backward pass (allocated on first use)
+    uint32_t* grad_deferred = nullptr;  // [1 + max_n] count, then the slots swept in double (same)
     // stage profiling: events 0..7 on the frame's stream
     bool profiling = false;
     cudaEvent_t ev_prof[8] = {};
@@ -117,7 +118,7 @@ struct spl_renderer {
 
 
     void release() {
-        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes); dfree(grad_rec);
+        dfree(keys_a); dfree(keys_b); dfree(vals_a); dfree(vals_b); dfree(idx); dfree(rec); dfree(boxes); dfree(grad_rec); dfree(grad_deferred);
         dfree(st_cull); dfree(st_bin);
         dfree(pk_a); dfree(pk_b); dfree(pv_a); dfree(pv_b);
         dfree(fc); dfree(fc_sort); dfree(coop_cnt); dfree(epoch); dfree(ranges); dfree(tile_order); dfree(d_u); dfree(d_sv);

@@ -125,12 +125,13 @@ void launch_activate_backward(uint32_t n, const float* quats, const float* logs,
                               const float* grot, const float* gsa, float* g_means, float* g_quats, float* g_logs,
                               float* g_logits, cudaStream_t st);
 // Backward of the last frame (fp32 blend): raster backward into grad_rec (10 floats per record),
-// then the vertex-stage backward into per-splat parameter gradients.
+// then the vertex-stage backward into per-splat parameter gradients.  deferred: 1 + max_n words (the
+// needles and discs whose vertex-stage sweep runs in double).
 void launch_backward(int sh_order, bool covariance, bool rect, const SceneView& s, const Uniforms& u,
                      const uint32_t* idx, const FrameCounters* fc, const uint2* boxes, const uint2* ranges,
                      const uint32_t* tile_order, const uint32_t* pair_vals, const float4* rec, const float4* image,
                      const float4* grad_image,
-                     float* grad_rec,
+                     float* grad_rec, uint32_t* deferred,
                      uint32_t max_n, float* gx, float* gy, float* gz, float4* grot, float4* gscale_alpha, float* gsh,
                      bool accumulate, cudaStream_t st);
 void launch_histogram(const uint32_t* keys, const uint32_t* n_ptr, uint32_t n_cap, uint32_t* hist4x256,

@@ -118,6 +118,155 @@ def test_off_axis_sphere_silhouette_is_tangent_cone():
         assert abs(ang - alpha) < 1e-6
 
 
+def _quat_matrix(q):
+    # the rotation matrix of the unit quaternion q = (scalar, i, j, k), textbook form
+    w, x, y, z = (float(c) for c in q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+KAT_CAMERAS = [([0.0, 0.0, 0.0], [0.0, 0.0, 1.0]), ([1.0, 2.0, -3.0], [0.0, 0.5, 4.0]),
+               ([-4.0, 1.5, 2.0], [3.0, -1.0, 1.0])]
+
+
+def _random_ellipsoids(u, count, seed):
+    """Unit-quaternion ellipsoids (scales 0.05-0.6, up to 12:1) in front of the camera, inside the view,
+    with their centres, rotations and scales as f32 (what the oracle reads)."""
+    rng = np.random.default_rng(seed)
+    cam = np.asarray(u["camera"][0], np.float64).reshape(4, 4)  # column-major: rows are the columns
+    C, eye = cam[:3, :3].T, cam[3, :3]
+    zc = rng.uniform(4.0, 12.0, count)
+    local = np.stack([rng.uniform(-0.5, 0.5, count) * zc, rng.uniform(-0.35, 0.35, count) * zc, zc], 1)
+    centers = (eye[None, :] + local @ C.T).astype(np.float32)
+    q = rng.normal(size=(count, 4))
+    q = (q / np.linalg.norm(q, axis=1, keepdims=True)).astype(np.float32)
+    scales = np.exp(rng.uniform(math.log(0.05), math.log(0.6), (count, 3))).astype(np.float32)
+    return centers, q, scales, C, eye
+
+
+def _outline(dbg, theta):
+    """Points of the oracle's outline ellipse (view plane z = 1): centre t, semi-axis a0 along
+    (k, -j) and a1 along (j, k), rotation (j, k)."""
+    t, (j, k), (a0, a1) = dbg[9:11], dbg[11:13], dbg[13:15]
+    U, V = np.array([k, -j]), np.array([j, k])
+    return t[None, :] + np.cos(theta)[:, None] * a0 * U[None, :] + np.sin(theta)[:, None] * a1 * V[None, :]
+
+
+@pytest.mark.parametrize("cam_i", range(len(KAT_CAMERAS)))
+def test_rotated_ellipsoid_outlines_lie_on_the_tangent_cone(cam_i):
+    # General rotated, off-axis ellipsoids seen from three cameras: every point of the extracted outline
+    # (extractTranslationOfEllipse, extractRotationOfEllipse with its sign fix-ups, extractScaleOfEllipse;
+    # shaders.wgsl:179-237) must lie on the cone of rays from the camera tangent to the ellipsoid.  A ray
+    # x = eye + s d meets (x - m)^T Q (x - m) = 1 (Q = R S^-2 R^T) in one point iff
+    # (d.Q w)^2 = (d.Q d)(w.Q w - 1), w = eye - m; the view-plane point p is the ray d = C (p, 1).
+    # An axis swapped between the two directions, a wrong sign fix-up or a wrong centre puts the sampled
+    # points off the cone.
+    cam = camera.look_at(*KAT_CAMERAS[cam_i])
+    u = oracle.uniforms(cam, 640, 480)
+    centers, q, scales, C, eye = _random_ellipsoids(u, 60, seed=100 + cam_i)
+    s60 = np.zeros((len(centers), 60), np.float32)
+    s60[:, 0:4], s60[:, 4:7], s60[:, 8:11], s60[:, 11] = q, centers, scales, 1.0
+    sc = scene_from_splats60(s60)
+    cfg = oracle.config_struct(use_covariance_for_scale=False, sh_order=0)
+    _, dbg, nv = oracle.preprocess(u, cfg, sc, np.arange(len(centers), dtype=np.uint32), fp64=True)
+    assert nv == len(centers)
+    theta = np.linspace(0.0, 2.0 * math.pi, 48, endpoint=False)
+    worst = 0.0
+    for i in range(len(centers)):
+        R = _quat_matrix(q[i].astype(np.float64))
+        Q = R @ np.diag(1.0 / scales[i].astype(np.float64) ** 2) @ R.T
+        w = eye - centers[i].astype(np.float64)
+        wqw = w @ Q @ w - 1.0
+        assert wqw > 0.0  # the camera is outside the ellipsoid
+        p = _outline(dbg[i], theta)
+        d = np.concatenate([p, np.ones((len(theta), 1))], 1) @ C.T
+        dqd = np.einsum("ni,ij,nj->n", d, Q, d)
+        dqw = d @ Q @ w
+        worst = max(worst, float(np.max(np.abs(dqw * dqw - dqd * wqw) / (dqd * wqw))))
+    assert worst < 1e-9
+
+
+@pytest.mark.parametrize("rect", [True, False], ids=["rect", "square"])
+def test_texture_coordinates_of_the_outline_closed_form(rect):
+    # The record's affine map tc = A (X, Y) + B at pixel position (X, Y) is the inverse of the quad basis
+    # [X Y] = [(k, -j)(bias + a0), (j, k)(bias + a1)] applied to the view-plane offset from the centre
+    # (shaders.wgsl:543-571: the rectangle maps its corners, the axis-aligned square applies `inverse` to
+    # its corner offsets; both interpolate affinely).  So a point of the outline at angle theta has
+    # tc = (a0 cos theta / (bias + a0), a1 sin theta / (bias + a1)), with the pixel position
+    # X = (p_x + vw) W / (2 vw), Y = (vh - p_y) H / (2 vh).  The square's half-size is
+    # margin * max(bias + a0, bias + a1) and its offsets (bx, by) = (-vw - t_x, vh - t_y)
+    # (shaders.wgsl:567-570); the rectangle's pixel box spans margin * (|X_x| + |Y_x|) horizontally.
+    cam = camera.look_at(*KAT_CAMERAS[1])
+    W, H = 640, 480
+    u = oracle.uniforms(cam, W, H)
+    centers, q, scales, C, eye = _random_ellipsoids(u, 40, seed=7)
+    s60 = np.zeros((len(centers), 60), np.float32)
+    s60[:, 0:4], s60[:, 4:7], s60[:, 8:11], s60[:, 11] = q, centers, scales * 4.0, 1.0
+    sc = scene_from_splats60(s60)
+    cfg = oracle.config_struct(use_covariance_for_scale=False, use_unaligned_rectangles=rect, sh_order=0)
+    rec, dbg, nv = oracle.preprocess(u, cfg, sc, np.arange(len(centers), dtype=np.uint32), fp64=True)
+    vw, vh = (float(x) for x in u["view_size"][0])
+    bias, margin = float(u["bias"][0]), float(u["margin"][0])
+    theta = np.linspace(0.0, 2.0 * math.pi, 36, endpoint=False)
+    checked = 0
+    for i in range(len(centers)):
+        t, (j, k), (a0, a1) = dbg[i, 9:11], dbg[i, 11:13], dbg[i, 13:15]
+        p = _outline(dbg[i], theta)
+        X = (p[:, 0] + vw) * W / (2.0 * vw)
+        Y = (vh - p[:, 1]) * H / (2.0 * vh)
+        r = rec[i].astype(np.float64)
+        tc = np.stack([r[0] * X + r[1] * Y + r[2], r[3] * X + r[4] * Y + r[5]], 1)
+        want = np.stack([a0 * np.cos(theta) / (bias + a0), a1 * np.sin(theta) / (bias + a1)], 1)
+        assert np.max(np.abs(tc - want)) < 1e-4
+        if rect:
+            assert r[12] == 0.0 and r[13] == 0.0 and r[14] == 0.0
+            ex = margin * (abs(k * (bias + a0)) + abs(j * (bias + a1)))
+        else:
+            assert r[14] == pytest.approx(margin * max(bias + a0, bias + a1), rel=1e-6)
+            assert r[12] == pytest.approx(-vw - t[0], rel=1e-6, abs=1e-7)
+            assert r[13] == pytest.approx(vh - t[1], rel=1e-6, abs=1e-7)
+            ex = float(r[14])
+        lo, hi = rec[i, 7:8].view(np.uint32)[0], rec[i, 11:12].view(np.uint32)[0]
+        if lo == 0xFFFFFFFF:
+            continue  # entirely outside the image
+        checked += 1
+        x0, x1 = int(lo & 0xFFFF), int(hi & 0xFFFF)
+        cxp, exp_ = (t[0] + vw) * W / (2.0 * vw), ex * W / (2.0 * vw)
+        # pixel centres x + 0.5 in [cxp - exp_, cxp + exp_] (to 1/64 px), clamped to the image
+        assert x0 == max(0, math.ceil(cxp - exp_ - 0.5 - 1.0 / 64)) or x0 == max(0, math.ceil(cxp - exp_ - 0.5))
+        assert x1 == min(W - 1, math.floor(cxp + exp_ - 0.5 + 1.0 / 64)) or x1 == min(W - 1, math.floor(cxp + exp_ - 0.5))
+        # the outline (margin 2 > 1) lies inside the box
+        inside = (X >= x0) & (X <= x1 + 1)
+        assert inside[(X >= 0) & (X <= W)].all()
+    assert checked >= 30
+
+
+def test_covariance_semi_axes_closed_form():
+    # use_covariance_for_scale: the semi-axes are the square roots of the eigenvalues of the 2x2 covariance
+    # J (C^T Sigma C) J^T, Sigma = R S^2 R^T, J the perspective Jacobian at the centre's camera coordinates
+    # v = view (m, 1) (with v_x / v_z and v_y / v_z clamped to [-1, 1]) (shaders.wgsl:99-118, 240-246).
+    cam = camera.look_at(*KAT_CAMERAS[2])
+    u = oracle.uniforms(cam, 640, 480)
+    centers, q, scales, C, eye = _random_ellipsoids(u, 60, seed=11)
+    s60 = np.zeros((len(centers), 60), np.float32)
+    s60[:, 0:4], s60[:, 4:7], s60[:, 8:11], s60[:, 11] = q, centers, scales, 1.0
+    sc = scene_from_splats60(s60)
+    cfg = oracle.config_struct(use_covariance_for_scale=True, sh_order=0)
+    _, dbg, _ = oracle.preprocess(u, cfg, sc, np.arange(len(centers), dtype=np.uint32), fp64=True)
+    view = np.asarray(u["view"][0], np.float64).reshape(4, 4).T  # the f32 view matrix, row-major
+    assert np.allclose(view[:3, :3], C.T, atol=1e-6)  # the camera's inverse
+    for i in range(len(centers)):
+        R = _quat_matrix(q[i].astype(np.float64))
+        sigma = R @ np.diag(scales[i].astype(np.float64) ** 2) @ R.T
+        v = view[:3, :3] @ centers[i].astype(np.float64) + view[:3, 3]
+        vx, vy = np.clip(v[0] / v[2], -1, 1) * v[2], np.clip(v[1] / v[2], -1, 1) * v[2]
+        J = np.array([[1 / v[2], 0.0, -vx / v[2] ** 2], [0.0, 1 / v[2], -vy / v[2] ** 2]])
+        P = J @ (C.T @ sigma @ C) @ J.T
+        want = np.sqrt(np.sort(np.linalg.eigvalsh(P))[::-1])
+        assert dbg[i, 13:15] == pytest.approx(want, rel=1e-9)
+
+
 def test_sh_band0_and_direction_terms():
     sh = np.zeros(48, np.float32)
     sh[0:3] = (1.0, -0.5, 0.25)

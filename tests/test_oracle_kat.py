@@ -357,6 +357,50 @@ def test_blend_single_splat_unorm8():
     assert img[0, 0].tolist() == [0, 0, 0, 255]  # cleared to (0, 0, 0, 1), renderer.rs:441-442
 
 
+@pytest.mark.parametrize("depth_sorting", [0, 1, 2, 3], ids=["none", "cpu", "gpu", "gpu-indirect"])
+@pytest.mark.parametrize("blend_mode", [0, 1], ids=["unorm8", "fp32"])
+def test_blend_two_splats_order_and_equation(depth_sorting, blend_mode):
+    # Two splats centred on the centre pixel (tc = 0 there, so each contributes its full alpha): the far
+    # one has index 0, the near one index 1.  The blend state (renderer.rs:260-270) is
+    #   C' = src_rgb * dst_a + C,   A' = A * (1 - src_a),   cleared to (0, 0, 0, 1) (renderer.rs:442),
+    # with the fragment's (rgb * alpha, alpha) clamped to [0, 1].  For the 8-bit target the blend runs
+    # in f32 against the stored k / 255 and each result is rounded to the nearest k (ties to even: with
+    # alpha 0.7f the transmittance (1 - 0.7f) * 255 is 76.5 in f32 and stores 76).  A sorted mode draws
+    # near to far; DepthSorting::None draws in index order (renderer.rs:14-22), here far first.
+    cam = camera.look_at([0.0, 0.0, 0.0], [0.0, 0.0, 1.0])
+    u = oracle.uniforms(cam, 33, 33)
+    th = math.radians(30.0)
+    q = [math.cos(th / 2), 0.0, 0.0, math.sin(th / 2)]
+    s60 = np.zeros((2, 60), np.float32)
+    s60[:, 0:4] = q
+    s60[0, 4:7], s60[1, 4:7] = [0.0, 0.0, 7.0], [0.0, 0.0, 4.0]
+    s60[:, 8:11] = [1.0, 1.2, 0.5]
+    s60[0, 11], s60[1, 11] = 0.7, 0.6
+    s60[0, 12:15], s60[1, 12:15] = [0.3, 0.8, -1.0], [1.0, -0.5, 0.2]
+    sc = scene_from_splats60(s60)
+    img, st = oracle.render(u, oracle.config_struct(depth_sorting=depth_sorting, sh_order=0,
+                                                    blend_mode=blend_mode), sc)
+    c0 = np.float32(0.28209479177387814)
+    rgb = [np.float32(0.5) + c0 * s60[i, 12:15] for i in range(2)]
+    order = [0, 1] if depth_sorting == 0 else [1, 0]
+    f, one, k255 = np.float32, np.float32(1.0), np.float32(255.0)
+    C, A = np.zeros(3, np.float32), one
+    for i in order:
+        a = s60[i, 11]
+        src = np.clip(rgb[i] * a, f(0), one)
+        if blend_mode == 0:  # stored as k / 255
+            C = np.rint(np.clip(src * A + C, f(0), one) * k255) / k255
+            A = np.rint(np.clip(A * (one - a), f(0), one) * k255) / k255
+        else:
+            C, A = src * A + C, A * (one - a)
+    px = img[16, 16]
+    if blend_mode == 0:
+        assert px.tolist() == [int(x) for x in np.rint(np.append(C, A) * k255)]
+    else:
+        assert np.allclose(px, list(C) + [A], rtol=0, atol=1e-6)
+    assert st[2] == 2  # both drawn
+
+
 def test_dev_scene_golden():
     """Pins the restatement against the committed golden image of the reference's dev-test scene
     (Scene::new_dev_test, scene.rs:158-192), produced by tests/golden/make_golden.py."""

@@ -228,7 +228,8 @@ SPL_API int spl_scene_wrap(spl_renderer* r, uint64_t splat_count, float* x, floa
  * respect to the splat parameters, given the frame's float4 image (r, g, b, T) and dL/d(image)
  * (float4 per pixel).  Writes, for every splat that was drawn, grad_x/y/z[i], grad_rotation[i][4],
  * grad_scale_alpha[i][4] (scale xyz, opacity) and grad_sh[i][48]; splats that were not drawn are left
- * untouched (zero the arrays first).  Transmittance is recomputed per tile, not stored; depth order,
+ * untouched (zero the arrays first).  grad_rotation, grad_scale_alpha and grad_sh must be 16-byte
+ * aligned (SPL_ERR_INVALID otherwise).  Transmittance is recomputed per tile, not stored; depth order,
  * culling and the 1/255 discard are treated as constants.  Asynchronous on `stream`. */
 SPL_API int spl_render_backward(spl_renderer* r, const spl_scene* scene, const float* image_device,
                                 const float* grad_image_device, float* grad_x, float* grad_y, float* grad_z,

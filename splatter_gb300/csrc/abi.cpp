@@ -524,6 +524,9 @@ static int render_backward(spl_renderer* r, const spl_scene* scene, const float*
     if (!r || !scene || !image_device || !grad_image_device || !grad_x || !grad_y || !grad_z || !grad_rotation ||
         !grad_scale_alpha || !grad_sh)
         return fail(SPL_ERR_INVALID, "NULL argument");
+    if ((reinterpret_cast<uintptr_t>(grad_rotation) | reinterpret_cast<uintptr_t>(grad_scale_alpha) |
+         reinterpret_cast<uintptr_t>(grad_sh)) & 15u)
+        return fail(SPL_ERR_INVALID, "grad_rotation, grad_scale_alpha and grad_sh must be 16-byte aligned");
     if (r->cfg.blend_mode != SPL_BLEND_FP32) return fail(SPL_ERR_INVALID, "the backward pass needs blend_mode FP32");
     if (!r->has_frame || r->last_scene != scene)
         return fail(SPL_ERR_INVALID, "render this scene with spl_render_frame first (the backward reuses that frame)");

@@ -33,6 +33,34 @@ __global__ void k_zero_grad_rec(float* grad_rec, const FrameCounters* fc, uint32
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) grad_rec[i] = 0.0f;
 }
 
+// Sums 10 values over the 8 lanes of a lane group (lane index li = lane & 7) in three exchange steps
+// that halve the values each lane carries (5 + 3 + 2 shuffles instead of 3 per value): afterwards lane
+// li holds the group sum of value k0 in v0 and, for li = 0 and 4, of value k0 + 1 in v1.
+//   li: 0 -> 0, 1   1 -> 2   2 -> 3   3 -> 4   4 -> 5, 6   5 -> 7   6 -> 8   7 -> 9
+__device__ __forceinline__ uint32_t reduce10_over8(const float* g, uint32_t li, float& v0, float& v1) {
+    const bool h4 = (li & 4u) != 0u, h2 = (li & 2u) != 0u, h1 = (li & 1u) != 0u;
+    float a[5], b[3];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {  // keep values 5..9 (h4) or 0..4
+        const float send = h4 ? g[i] : g[i + 5], keep = h4 ? g[i + 5] : g[i];
+        a[i] = keep + __shfl_xor_sync(FULL_MASK, send, 4);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {  // keep a[3..4] (h2) or a[0..2]
+        const float hi = i < 2 ? a[i + 3] : 0.0f;
+        const float send = h2 ? a[i] : hi, keep = h2 ? hi : a[i];
+        b[i] = keep + __shfl_xor_sync(FULL_MASK, send, 2);
+    }
+    // h2 lanes carry two values (b0, b1): keep b1 (h1) or b0; the others three: keep b2 (h1) or b0, b1
+    const float send0 = h1 ? b[0] : (h2 ? b[1] : b[2]);
+    const float keep0 = h1 ? (h2 ? b[1] : b[2]) : b[0];
+    const float send1 = (h1 && !h2) ? b[1] : 0.0f;
+    const float keep1 = (!h1 && !h2) ? b[1] : 0.0f;
+    v0 = keep0 + __shfl_xor_sync(FULL_MASK, send0, 1);
+    v1 = keep1 + __shfl_xor_sync(FULL_MASK, send1, 1);
+    return (h4 ? 5u : 0u) + (h2 ? (h1 ? 4u : 3u) : (h1 ? 2u : 0u));
+}
+
 template <bool RECT>
 __global__ void __launch_bounds__(256) k_raster_backward(const uint2* __restrict__ ranges,
                                                          const uint32_t* __restrict__ tile_order,
@@ -146,10 +174,10 @@ __global__ void __launch_bounds__(256) k_raster_backward(const uint2* __restrict
                                     }
                                     const float om = 1.0f - sa;
                                     float dsa = 0.0f;
-                                    if (om > 0.0f) {
+                                    if (om > 0.0f) {  // om in (0, 1]: the fast divide is within 2 ulp
                                         const float Sdot =
                                             (gC[0] * (Cf[0] - Ca[0]) + gC[1] * (Cf[1] - Ca[1])) + gC[2] * (Cf[2] - Ca[2]);
-                                        dsa = -(Sdot + kT) / om;
+                                        dsa = __fdividef(-(Sdot + kT), om);
                                     }
                                     T = T * om;
                                     done = T < FP32_T_MIN;
@@ -179,21 +207,14 @@ __global__ void __launch_bounds__(256) k_raster_backward(const uint2* __restrict
                         }
                     }
                     // reduce over the 8 lanes of the group (all hold the same record this iteration)
-                    const bool any = __any_sync(FULL_MASK, contrib);
-                    if (any) {
-#pragma unroll
-                        for (int k = 0; k < GR; ++k) {
-                            float v = g[k];
-                            v += __shfl_xor_sync(FULL_MASK, v, 4);
-                            v += __shfl_xor_sync(FULL_MASK, v, 2);
-                            v += __shfl_xor_sync(FULL_MASK, v, 1);
-                            g[k] = v;
-                        }
-                        const uint32_t gm = __ballot_sync(FULL_MASK, contrib);
-                        if (li == 0 && ((gm >> (grp * 8u)) & 0xFFu)) {
+                    const uint32_t gm = __ballot_sync(FULL_MASK, contrib);
+                    if (gm != 0u) {
+                        float v0, v1;
+                        const uint32_t k0 = reduce10_over8(g, li, v0, v1);
+                        if ((gm >> (grp * 8u)) & 0xFFu) {
                             float* dst = grad_rec + (size_t)s_slot[j] * GR;
-#pragma unroll
-                            for (int k = 0; k < GR; ++k) atomicAdd(dst + k, g[k]);
+                            atomicAdd(dst + k0, v0);
+                            if ((li & 3u) == 0u) atomicAdd(dst + k0 + 1u, v1);
                         }
                     }
                 }
@@ -216,10 +237,18 @@ struct VjpInputs {
         cz = __ldg(s.z + i);
         rot = __ldg(s.rot + i);
         sca = __ldg(s.scale_alpha + i);
-        constexpr int NF = 3 * (SHO + 1) * (SHO + 1);
-        const float* p = s.sh + (size_t)i * 48;
+        // 16-byte loads of the row's first NF coefficients (rows are 192 bytes, 16-byte aligned; the
+        // last load of SH degree 2 also reads coefficient 27, inside the row)
+        constexpr int NF4 = (3 * (SHO + 1) * (SHO + 1) + 3) / 4;
+        const float4* p = reinterpret_cast<const float4*>(s.sh + (size_t)i * 48);
 #pragma unroll
-        for (int k = 0; k < NF; ++k) sh[k] = __ldg(p + k);
+        for (int k = 0; k < NF4; ++k) {
+            const float4 v = __ldg(p + k);
+            sh[4 * k + 0] = v.x;
+            sh[4 * k + 1] = v.y;
+            sh[4 * k + 2] = v.z;
+            sh[4 * k + 3] = v.w;
+        }
         const float Xr = 0.5f * (float)((bb.x & 0xFFFFu) + (bb.y & 0xFFFFu) + 1u);
         const float Yr = 0.5f * (float)((bb.x >> 16) + (bb.y >> 16) + 1u);
         const float vw = u.view_size[0], vh = u.view_size[1];
@@ -229,12 +258,14 @@ struct VjpInputs {
 };
 
 __device__ __forceinline__ bool load_record_gradient(const float* grad_rec, uint32_t slot, float* g) {
-    const float* gr = grad_rec + (size_t)slot * GR;
+    const float2* gr = reinterpret_cast<const float2*>(grad_rec + (size_t)slot * GR);  // 40-byte rows
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < GR; ++k) {
-        g[k] = gr[k];
-        any = any || g[k] != 0.0f;
+    for (int k = 0; k < GR / 2; ++k) {
+        const float2 v = gr[k];
+        g[2 * k] = v.x;
+        g[2 * k + 1] = v.y;
+        any = any || v.x != 0.0f || v.y != 0.0f;
     }
     return any;  // false: not drawn, or no gradient reached it
 }
@@ -289,23 +320,24 @@ __global__ void __launch_bounds__(128, 3) k_preprocess_backward(SceneView s, Uni
         const float len = sqrtf((vx * vx + vy * vy) + vz * vz);
         float B[16];
         sh_basis<SHO>(vx / len, vy / len, vz / len, B);
+        // coefficient m = 3 k + c gets B[k] g[7 + c]: whole 16-byte groups, then the tail
+        constexpr int NF = 3 * (SHO + 1) * (SHO + 1), NV = NF / 4;
+        float v[NF];
+#pragma unroll
+        for (int m = 0; m < NF; ++m) v[m] = B[m / 3] * g[7 + m % 3];
         float* o = gsh + (size_t)i * 48;
-        constexpr int NK = (SHO + 1) * (SHO + 1);
-        if (accumulate) {
+        float4* o4 = reinterpret_cast<float4*>(o);
 #pragma unroll
-            for (int k = 0; k < NK; ++k) {
-                o[3 * k + 0] += B[k] * g[7];
-                o[3 * k + 1] += B[k] * g[8];
-                o[3 * k + 2] += B[k] * g[9];
+        for (int k = 0; k < NV; ++k) {
+            float4 x = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            if (accumulate) {
+                const float4 y = o4[k];
+                x = make_float4(y.x + x.x, y.y + x.y, y.z + x.z, y.w + x.w);
             }
-        } else {
-#pragma unroll
-            for (int k = 0; k < NK; ++k) {
-                o[3 * k + 0] = B[k] * g[7];
-                o[3 * k + 1] = B[k] * g[8];
-                o[3 * k + 2] = B[k] * g[9];
-            }
+            o4[k] = x;
         }
+#pragma unroll
+        for (int m = 4 * NV; m < NF; ++m) o[m] = accumulate ? o[m] + v[m] : v[m];
     }
 }
 

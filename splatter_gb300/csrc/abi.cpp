@@ -369,7 +369,7 @@ static int render_frame_impl(spl_renderer* r, const SceneView& sv, const Uniform
     const int passes = tiles <= 256 ? 1 : (tiles <= 65536 ? 2 : 3);
     if (coop) {
         CU(launch_sort_coop(r->pk_a, r->pk_b, r->pv_a, r->pv_b, false, &r->fc->pairs, (uint32_t)r->pair_cap, passes,
-                            0, r->coop_cnt, r->fc->barrier, sl, &r->fc->err, st));
+                            0, r->coop_cnt, r->fc->barrier + 1, sl, &r->fc->err, st));
     } else {
         // tile-id histograms from the binning kernel
         uint32_t *ak = r->pk_a, *av = r->pv_a, *bk = r->pk_b, *bv = r->pv_b;

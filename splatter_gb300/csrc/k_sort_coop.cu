@@ -16,7 +16,9 @@
 //   5. bounded grid barrier (the next pass reads this pass's output)
 // The ranking keeps equal digits in input order, so every pass is stable, like the onesweep passes.
 // Every barrier wait is bounded: on timeout the error bit is raised and the kernel runs to its end
-// (writes stay in bounds), so a missing CTA can never hang the GPU.
+// (writes stay in bounds), so a missing CTA can never hang the GPU.  The barrier word counts the
+// launch's arrivals and must be zero when the launch starts (each sort of a frame has its own word in
+// the frame counters, which the frame start zeroes).
 #include "spl_device.cuh"
 
 namespace spl {
@@ -43,26 +45,26 @@ struct CoopSmem {
     uint32_t scan[CS_WARPS];
 };
 
-__device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t spin_limit, uint32_t* err) {
+// Grid barrier on a word that only counts arrivals (zero when the launch starts): the b-th barrier of
+// the launch (b = 0, 1, ...) waits until *bar reaches (b + 1) * nblocks.  Releasing takes only the
+// last arrival's atomic: no reset and no generation word on the critical path (those cost two more
+// L2 round trips per barrier).
+__device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t target, uint32_t spin_limit, uint32_t* err) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile uint32_t* vgen = bar + 1;
-        const uint32_t gen = *vgen;
         __threadfence();
-        const uint32_t arrived = atomicAdd(bar, 1u);
-        if (arrived == nblocks - 1u) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            uint32_t spins = 0;
-            while (*vgen == gen) {
-                if (++spins > spin_limit) {
-                    atomicOr(err, SPL_DEV_ERR_LOOKBACK);
-                    break;
-                }
-                if (spins > 32) __nanosleep(32);
+        atomicAdd(bar, 1u);
+        const volatile uint32_t* v = bar;
+        uint32_t spins = 0;
+        while (*v < target) {
+            if (++spins > spin_limit) {
+                atomicOr(err, SPL_DEV_ERR_LOOKBACK);
+                break;
             }
+            // a barrier of this launch already timed out: the later ones would too, each after its own
+            // spin limit; stop waiting (the frame reports the error)
+            if ((spins & 1023u) == 0u && (*(volatile uint32_t*)err & SPL_DEV_ERR_LOOKBACK)) break;
+            if (spins > 32) __nanosleep(32);
         }
         __threadfence();
     }
@@ -231,6 +233,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
         return;
     }
     const uint32_t Gp = (G + 3u) & ~3u;  // padded row stride of cnt (16-byte rows)
+    uint32_t bar_target = 0u;             // arrivals that release the next grid barrier
     uint32_t* tot = cnt + (size_t)256 * Gp;  // per-digit totals of a pass
     const uint32_t s_begin = c * seg, s_end = min(s_begin + seg, n);
     for (int p = 0; p < passes; ++p) {
@@ -287,7 +290,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
             cnt[(size_t)tid * Gp + c] = acc;
         }
         __syncthreads();
-        grid_barrier(bar, G, spin_limit, err);
+        grid_barrier(bar, bar_target += G, spin_limit, err);
         // ---- 3a. distributed scan: digit row d of cnt[d][0..G) becomes its exclusive prefix over
         //          the CTAs and its total goes to tot[d].  The rows are dealt round robin over the
         //          CTAs, so every row's loads are in flight at once (one L2 round trip): with at most
@@ -339,7 +342,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
                 if (lane == 31u) tot[d] = x;
             }
         }
-        grid_barrier(bar, G, spin_limit, err);
+        grid_barrier(bar, bar_target += G, spin_limit, err);
         // ---- 3b. offsets: this CTA's column of prefixes plus the global digit bases ----
         {
             uint32_t dtotal = 0, dpre = 0;
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(CS_THREADS, 2)
             if (tid < 256) sm.running[tid] += sm.tcount[tid];
         }
         // ---- 5. the next pass reads this pass's output ----
-        grid_barrier(bar, G, spin_limit, err);
+        grid_barrier(bar, bar_target += G, spin_limit, err);
     }
 }
 

@@ -38,7 +38,7 @@ struct FrameCounters {
     uint32_t err;              // SPL_DEV_ERR_* bits
     uint32_t draw;             // entries drawn (mode dependent)
     uint32_t epoch;            // copy of the frame epoch (for readback)
-    uint32_t barrier[2];       // grid barrier of the cooperative sort: arrivals, generation
+    uint32_t barrier[2];       // grid-barrier arrivals of the cooperative depth sort and pair sort
     uint32_t hist_depth[4][256];  // digit histograms of the visible depth keys (onesweep sort only)
     uint32_t hist_pairs[3][256];  // digit histograms of the tile ids of all pairs (onesweep sort only)
 };
@@ -112,7 +112,8 @@ void launch_soa_to_splats60(const SceneView& s, uint32_t start, uint32_t count, 
 void launch_gather_entries(const uint32_t* keys, const uint32_t* slots, const uint32_t* idx, const FrameCounters* fc,
                            int mode, uint32_t* keys_out, uint32_t* idx_out, uint32_t cap, cudaStream_t st);
 // All passes of a stable LSD radix sort in one cooperative launch (k_sort_coop.cu).  Pass p reads
-// buffers (p even: 0, odd: 1) and writes the other; cnt holds 256 x sort_coop_grid() words.
+// buffers (p even: 0, odd: 1) and writes the other; cnt holds 256 x sort_coop_grid() words; *bar (the
+// grid barrier's arrival count) must be zero when the launch starts.
 cudaError_t launch_sort_coop(uint32_t* keys0, uint32_t* keys1, uint32_t* vals0, uint32_t* vals1, bool iota_first,
                              const uint32_t* n_ptr, uint32_t n_cap, int passes, int shift0, uint32_t* cnt,
                              uint32_t* bar, uint32_t spin_limit, uint32_t* err, cudaStream_t st);

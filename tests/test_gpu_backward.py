@@ -327,6 +327,40 @@ def test_needle_gradients_are_repeatable(cuda, gap):
             assert float((a - b).abs().max()) <= 5e-6 * float(a.abs().max())
 
 
+def test_backward_rejects_unaligned_gradient_arrays(cuda):
+    """spl_render_backward writes rotation, scale/opacity and SH gradients with 16-byte stores: an output
+    array that is not 16-byte aligned is refused with SPL_ERR_INVALID before anything is launched, and
+    aligned arrays of the same frame are accepted."""
+    import ctypes
+    import torch
+    from splatter_gb300 import SplatterError
+    from splatter_gb300._lib import check
+    n, W, H = 2000, 64, 48
+    rec, cam, cfg = _setup(n, W, H, seed=71, scale_boost=1.0)
+    r = Renderer(cfg)
+    sc = Scene(r, n)
+    sc.load_chunk(rec)
+    img = r.render_frame(sc, cam, W, H).contiguous()
+    g = torch.ones_like(img)
+    xyz = torch.zeros((3, n), device="cuda")
+    # one buffer per array, a float longer than it: element 0 is aligned, element 1 is 4 bytes off
+    bufs = [torch.zeros(k * n + 4, device="cuda") for k in (4, 4, 48)]
+    aligned = [b[:k * n] for b, k in zip(bufs, (4, 4, 48))]
+    shifted = [b[1:k * n + 1] for b, k in zip(bufs, (4, 4, 48))]
+    assert all(t.data_ptr() % 16 == 0 for t in aligned) and all(t.data_ptr() % 16 == 4 for t in shifted)
+
+    def call(arrays):
+        p = [ctypes.c_void_p(t.data_ptr()) for t in (img, g, xyz[0], xyz[1], xyz[2], *arrays)]
+        check(r._lib.spl_render_backward(r.handle, sc.handle, *p, None))
+
+    for k in range(3):
+        with pytest.raises(SplatterError):
+            call([shifted[i] if i == k else aligned[i] for i in range(3)])
+    call(aligned)
+    torch.cuda.synchronize()
+    assert float(aligned[2].abs().sum()) > 0.0  # SH gradients were written
+
+
 def test_render_raw_views_equals_per_view_sum(cuda):
     """render_raw_views: the stacked frames equal render_raw's frame of each view bit for bit, and
     the in-place accumulated gradients equal the per-view render_raw gradients that autograd sums

@@ -267,6 +267,42 @@ def test_nonfinite_and_degenerate_inputs(cuda):
     assert_frame_parity(g, o, config)
 
 
+@pytest.mark.parametrize("covariance", [True, False], ids=["covariance", "ellipse"])
+def test_camera_inside_and_screen_filling_splats(cuda, covariance):
+    """Splats whose ellipsoid contains the camera (the bounding cone of shaders.wgsl:125-169 has no
+    real silhouette then), splats just beyond the near plane (view z = 1) that cover the whole
+    viewport (boxes clamped to the image, every tile binned), and splats whose centre sits at the near
+    plane, among ordinary ones: the same keys, visible set, records and image as the oracle, and no
+    device error."""
+    n = 20000
+    config = Configuration(spherical_harmonics_order=3, max_splat_count=n, field_of_view_y=math.radians(60),
+                           use_covariance_for_scale=covariance)
+    rec = synthetic.plain_small(n, seed=43, sh_order=3)
+    rec[:, 55:58] += 1.0
+    eye = np.array([0.3, 0.5, -7.0], np.float32)
+    cam = camera.look_at(eye, [0.0, 0.0, 0.0])
+    fwd = -eye / np.linalg.norm(eye)
+    rng = np.random.default_rng(44)
+    k = np.arange(0, n, 211)  # ~95 special splats
+    for j, i in enumerate(k):
+        kind = j % 3
+        if kind == 0:    # the camera inside: centre 1.2-1.5 ahead, radii ~e^1.5 = 4.5
+            rec[i, 0:3] = eye + fwd * float(rng.uniform(1.2, 1.5)) + rng.normal(0.0, 0.05, 3).astype(np.float32)
+            rec[i, 55:58] = 1.5 + rng.normal(0.0, 0.2, 3).astype(np.float32)
+        elif kind == 1:  # just beyond the near plane, filling the view
+            rec[i, 0:3] = eye + fwd * float(rng.uniform(1.1, 2.0)) + rng.normal(0.0, 0.05, 3).astype(np.float32)
+            rec[i, 55:58] = rng.uniform(-1.0, 0.5, 3).astype(np.float32)
+        else:            # centre at the near plane
+            rec[i, 0:3] = eye + fwd * float(rng.uniform(0.95, 1.05)) + rng.normal(0.0, 0.2, 3).astype(np.float32)
+            rec[i, 55:58] = rng.uniform(-1.0, 0.5, 3).astype(np.float32)
+        rec[i, 54] = -2.0  # low opacity, so that the scene behind stays visible
+    g = gpu_frame(cuda, config, rec, cam, 320, 240)
+    o = oracle_frame(config, oracle.load_transform(rec), cam, 320, 240)
+    assert g[3].device_error == 0
+    assert g[3].visible_count > 1000
+    assert_frame_parity(g, o, config)
+
+
 @pytest.mark.parametrize("w,h", [(1, 1), (17, 9), (1000, 3), (3, 700), (257, 255), (4112, 4112)])
 def test_viewports(cuda, w, h):
     """Viewports that are not multiples of the 16-pixel tile, degenerate strips, one pixel, and one

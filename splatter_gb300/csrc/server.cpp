@@ -5,7 +5,9 @@
 // scale+opacity, SH, x, y, z) and, while resident, one block from a stream-ordered device memory
 // pool.  Residency is admitted against `scene_memory_budget`; the least recently used scene with no
 // request in flight is evicted (its device block returned to the pool on the copy stream) and copied
-// back on its next request, the request's stream waiting on the copy's event.
+// back for its next request, the request's stream waiting on the copy's event: at the request's
+// admission, or earlier, while it still waits in the queue (up to two scenes of the next 2 x slots
+// queued requests, evicting none that those requests want).
 //
 // Requests: a FIFO queue filled by spl_server_submit from any thread.  One scheduler thread admits
 // the head request whenever a slot is free (continuous admission: no batch boundary), renders it on
@@ -50,6 +52,8 @@ struct ServerScene {
     cudaEvent_t ready = nullptr;    // the block's last copy to the device
     uint64_t last_use = 0;
     uint32_t in_flight = 0;
+    bool wanted = false;      // needed by one of the next queued requests (scheduler's lookahead window)
+    bool prefetched = false;  // copied back ahead of its request; the request that uses it reports it
 
     void point_view() {
         unsigned char* b = dev;
@@ -147,32 +151,37 @@ void CUDART_CB on_slot_done(void* p) {
 void evict(spl_server* s, ServerScene* sc) {
     cudaFreeAsync(sc->dev, s->copy_st);
     sc->dev = nullptr;
+    sc->prefetched = false;
     s->resident_bytes -= sc->bytes;
     s->evictions.fetch_add(1);
 }
 
-ServerScene* lru_victim(spl_server* s, const ServerScene* keep) {
+// The least recently used resident scene with no request in flight, preferring scenes that none of
+// the next queued requests wants; with `spare_wanted` the wanted ones are never chosen.
+ServerScene* lru_victim(spl_server* s, const ServerScene* keep, bool spare_wanted) {
     ServerScene* v = nullptr;
-    for (auto& c : s->scenes)
-        if (c->dev && c.get() != keep && c->in_flight == 0 && (!v || c->last_use < v->last_use)) v = c.get();
+    for (auto& c : s->scenes) {
+        if (!c->dev || c.get() == keep || c->in_flight != 0 || (spare_wanted && c->wanted)) continue;
+        if (!v || (v->wanted && !c->wanted) || (v->wanted == c->wanted && c->last_use < v->last_use)) v = c.get();
+    }
     return v;
 }
 
 // Evicts until `need` more bytes fit the budget; BLOCKED when the scenes in use leave no room yet.
-int make_room(spl_server* s, uint64_t need, const ServerScene* keep) {
+int make_room(spl_server* s, uint64_t need, const ServerScene* keep, bool spare_wanted) {
     const uint64_t budget = s->scfg.scene_memory_budget;
     if (!budget) return SPL_OK;
     if (need > budget) return spl::fail(SPL_ERR_CAPACITY, "scene of %llu bytes exceeds the scene memory budget",
                                         (unsigned long long)need);
     while (s->resident_bytes + need > budget) {
-        ServerScene* v = lru_victim(s, keep);
+        ServerScene* v = lru_victim(s, keep, spare_wanted);
         if (!v) return BLOCKED;
         evict(s, v);
     }
     return SPL_OK;
 }
 
-int alloc_block(spl_server* s, ServerScene* sc) {
+int alloc_block(spl_server* s, ServerScene* sc, bool spare_wanted) {
     for (;;) {
         cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&sc->dev), sc->bytes, s->pool, s->copy_st);
         if (e == cudaSuccess) return SPL_OK;
@@ -180,17 +189,18 @@ int alloc_block(spl_server* s, ServerScene* sc) {
         sc->dev = nullptr;
         if (e != cudaErrorMemoryAllocation) return spl::fail(SPL_ERR_CUDA, "cudaMallocFromPoolAsync: %s",
                                                              cudaGetErrorString(e));
-        ServerScene* v = lru_victim(s, sc);  // out of device memory below the budget: evict further
+        ServerScene* v = lru_victim(s, sc, spare_wanted);  // out of device memory below the budget: evict further
         if (!v) return BLOCKED;
         evict(s, v);
     }
 }
 
-// Copies an evicted scene back to the device (asynchronously, on the copy stream).
-int make_resident(spl_server* s, ServerScene* sc) {
-    int rc = make_room(s, sc->bytes, sc);
+// Copies an evicted scene back to the device (asynchronously, on the copy stream).  With
+// `spare_wanted` (a restore ahead of its request) no scene that a queued request wants is evicted.
+int make_resident(spl_server* s, ServerScene* sc, bool spare_wanted = false) {
+    int rc = make_room(s, sc->bytes, sc, spare_wanted);
     if (rc) return rc;
-    rc = alloc_block(s, sc);
+    rc = alloc_block(s, sc, spare_wanted);
     if (rc) return rc;
     CU(cudaMemcpyAsync(sc->dev, sc->host, sc->bytes, cudaMemcpyHostToDevice, s->copy_st));
     CU(cudaEventRecord(sc->ready, s->copy_st));
@@ -317,6 +327,9 @@ void admit(spl_server* s) {
             rc = make_resident(s, sc);
             if (rc == BLOCKED) return;
             restored = rc == SPL_OK;
+        } else if (sc->prefetched) {  // copied back ahead of this request
+            restored = true;
+            sc->prefetched = false;
         }
         {
             std::lock_guard<std::mutex> lk(s->q_mu);
@@ -334,6 +347,41 @@ void admit(spl_server* s) {
     }
 }
 
+// Marks the scenes of the next `window` queued requests as wanted (evicted last, never by a restore
+// ahead of a request) and returns their ids in queue order.
+std::vector<uint32_t> mark_wanted(spl_server* s, size_t window) {
+    std::vector<uint32_t> ids;
+    {
+        std::lock_guard<std::mutex> lk(s->q_mu);
+        for (size_t i = 0; i < s->queue.size() && ids.size() < window; ++i) ids.push_back(s->queue[i].req.scene_id);
+    }
+    for (auto& c : s->scenes) c->wanted = false;
+    for (uint32_t id : ids)
+        if (id < s->scenes.size()) s->scenes[id]->wanted = true;
+    return ids;
+}
+
+// With a scene memory budget: copies the scenes of the next queued requests back before those
+// requests are admitted, so that the copy engine works while the slots render (a restore at admission
+// leaves it idle until a slot frees).  At most two such restores wait for their requests at a time,
+// and none evicts a scene that a queued request in the window wants.
+void prefetch(spl_server* s) {
+    if (!s->scfg.scene_memory_budget) return;
+    const std::vector<uint32_t> ids = mark_wanted(s, 2 * s->slots.size());
+    int ahead = 0;
+    for (auto& c : s->scenes) ahead += c->prefetched ? 1 : 0;
+    for (uint32_t id : ids) {
+        if (ahead >= 2) break;
+        if (id >= s->scenes.size()) continue;
+        ServerScene* sc = s->scenes[id].get();
+        if (sc->dev) continue;
+        if (make_resident(s, sc, true) != SPL_OK) break;  // no room yet (an error is reported at admission)
+        sc->prefetched = true;
+        sc->last_use = ++s->use_tick;
+        ++ahead;
+    }
+}
+
 void scheduler(spl_server* s) {
     cudaSetDevice(s->device);
     for (;;) {
@@ -341,7 +389,9 @@ void scheduler(spl_server* s) {
         {
             std::lock_guard<std::mutex> g(s->sched_mu);
             retire(s);
+            if (s->scfg.scene_memory_budget) mark_wanted(s, 2 * s->slots.size());
             admit(s);
+            prefetch(s);
             bool any_busy = false;
             for (auto& o : s->slots) any_busy = any_busy || o->busy;
             std::lock_guard<std::mutex> lk(s->q_mu);
@@ -473,7 +523,7 @@ int spl_server_add_scene(spl_server* s, const float* records62, uint64_t count, 
     sc->view.owns = false;
     sc->view.n = sc->n;
     sc->view.device = s->device;
-    int rc = make_room(s, sc->bytes, nullptr);
+    int rc = make_room(s, sc->bytes, nullptr, false);
     if (rc == BLOCKED) return spl::fail(SPL_ERR_CAPACITY, "scenes in use leave no room for a new scene");
     if (rc) return rc;
     cudaError_t e = cudaEventCreateWithFlags(&sc->ready, cudaEventDisableTiming);
@@ -492,7 +542,7 @@ int spl_server_add_scene(spl_server* s, const float* records62, uint64_t count, 
         cudaGetLastError();
         return code;
     };
-    rc = alloc_block(s, sc.get());
+    rc = alloc_block(s, sc.get(), false);
     if (rc == BLOCKED) return undo(spl::fail(SPL_ERR_OOM, "no device memory for the scene"));
     if (rc) return undo(rc);
     sc->point_view();

@@ -540,13 +540,14 @@ def run_differentiation(args, iters=5, warmup=3, full=True):
     """Forward+backward ms/iter through torch.autograd (the loader's activations and the hand-written
     backward behind autograd Functions).  One iteration = the 8 views rendered, compared with their
     targets and back-propagated, gradients summed over the views: `ms_per_iter` with the 8 views in
-    one node (render_raw_views: one renderer per view, gradients added in place on the GPU),
+    one node (render_raw_views: one renderer per view, gradients added in place on the GPU) and the
+    L2 loss in one pass each way (l2_image_loss: the same value and gradient as the torch expression),
     `ms_per_iter_view_nodes` with one render_raw node and one backward call per view (autograd sums
     the per-view gradient arrays).  full=False times the one-node iteration alone."""
     import numpy as np
     import torch
     from splatter_gb300 import BlendMode, Configuration, Renderer, camera, synthetic
-    from splatter_gb300.autograd import render_raw, render_raw_views
+    from splatter_gb300.autograd import l2_image_loss, render_raw, render_raw_views
 
     n, W, H, views = 1_000_000, 1024, 1024, 8
     rec = synthetic.clustered(n, seed=args.seed + 11, sh_order=3)
@@ -589,7 +590,7 @@ def run_differentiation(args, iters=5, warmup=3, full=True):
         for t in leaves:
             t.grad = None
         imgs = render_raw_views(leaves[0], leaves[1], leaves[2], leaves[3], leaves[4], view_renderers, poses, W, H)
-        loss = ((imgs[..., :3] - target_stack) ** 2).sum()
+        loss = l2_image_loss(imgs, target_stack)  # ((imgs[..., :3] - target_stack) ** 2).sum(), fused
         loss.backward()
         return loss.detach()
 

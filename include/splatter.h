@@ -260,6 +260,17 @@ SPL_API int spl_activate_splats_backward(uint64_t n, const float* quaternions, c
                                          const float* grad_scale_alpha, float* grad_means, float* grad_quaternions,
                                          float* grad_log_scales, float* grad_opacity_logits, void* stream);
 
+/* The L2 image loss of a training loop, sum over pixels and RGB of (image - target)^2, for `pixels`
+ * float4 pixels (r, g, b, T; 16-byte aligned) against three floats per pixel: writes
+ * spl_l2_image_loss_partials(pixels) partial sums to `partial` (their sum is the loss).  Its backward
+ * writes grad_image[p] = (2 (image - target) * s, 0) with the scalar s (the loss's upstream gradient)
+ * read from device memory: one pass each, the values torch's autograd forms for the same expression.
+ * Asynchronous on `stream`. */
+SPL_API uint32_t spl_l2_image_loss_partials(uint64_t pixels);
+SPL_API int spl_l2_image_loss(const float* image, const float* target, uint64_t pixels, float* partial, void* stream);
+SPL_API int spl_l2_image_loss_backward(const float* image, const float* target, uint64_t pixels,
+                                       const float* scale_device, float* grad_image, void* stream);
+
 /* Copies the last backward pass's per-record gradients (10 floats per visible splat, compaction
  * order: d/dA00, d/dA01, d/dB0, d/dA10, d/dA11, d/dB1 with A taken against pixel offsets from the
  * centre of the record's pixel box and B at that centre, then d/dopacity, d/dr, d/dg, d/db) into a

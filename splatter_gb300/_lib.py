@@ -159,6 +159,9 @@ SIGNATURES = [
     ("spl_server_now_ns", U64, []),
     ("spl_activate_splats", I32, [U64, P, P, P, P, P, P, P, P, P, P]),
     ("spl_activate_splats_backward", I32, [U64, P, P, P, P, P, P, P, P, P, P, P, P, P, P]),
+    ("spl_l2_image_loss_partials", U32, [U64]),
+    ("spl_l2_image_loss", I32, [P, P, U64, P, P]),
+    ("spl_l2_image_loss_backward", I32, [P, P, U64, P, P, P]),
 ]
 
 NO_ALLOC_MAX_PAIRS = 262144

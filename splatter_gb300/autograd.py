@@ -8,9 +8,10 @@ log-scales clamped to mean +- 5, sigmoid of the opacity logit) with the loader's
 GPU (spl_activate_splats) and chains its backward there too (spl_activate_splats_backward), so
 gradients reach the raw parameters a training loop optimises without torch elementwise kernels per
 frame.  `render_raw_views` renders several views of the same raw parameters in one autograd node and
-sums their gradients in place on the GPU (spl_render_backward_accumulate).  `activate` is the same
-transform written in torch (a reference).  Depth order, culling and the 1/255 discard are constants
-of the frame (no gradient), as in any splat rasteriser.
+sums their gradients in place on the GPU (spl_render_backward_accumulate).  `l2_image_loss` is the
+L2 loss of such frames against RGB targets, one pass each way (spl_l2_image_loss).  `activate` is
+the same transform written in torch (a reference).  Depth order, culling and the 1/255 discard are
+constants of the frame (no gradient), as in any splat rasteriser.
 """
 import ctypes
 
@@ -20,7 +21,7 @@ from . import _lib
 from ._lib import check
 from .renderer import BlendMode, Renderer, _stream_ptr
 
-__all__ = ["render_splats", "render_raw", "render_raw_views", "activate", "activate_native"]
+__all__ = ["render_splats", "render_raw", "render_raw_views", "activate", "activate_native", "l2_image_loss"]
 
 
 def _ptr(t):
@@ -322,3 +323,48 @@ def render_raw_views(means, quats, log_scales, opacity_logits, sh, renderers, ca
             raise ValueError("render_raw_views: float32 CUDA tensors (N, 3), (N, 4), (N, 3), (N,), (N, 48) expected")
     return _RenderRawViews.get().apply(means, quats, log_scales, opacity_logits, sh, renderers, cameras, width,
                                        height)
+
+
+class _L2ImageLoss:  # built lazily, like _RenderSplats
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is None:
+            torch = _import_torch()
+
+            class L2ImageLoss(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, images, targets):
+                    images, targets = images.contiguous(), targets.contiguous()
+                    pixels = images.numel() // 4
+                    lib = _lib.load()
+                    partial = torch.empty(int(lib.spl_l2_image_loss_partials(pixels)), device=images.device,
+                                          dtype=torch.float32)
+                    check(lib.spl_l2_image_loss(_ptr(images), _ptr(targets), pixels, _ptr(partial), _stream_ptr(None)))
+                    ctx.save_for_backward(images, targets)
+                    return partial.sum()
+
+                @staticmethod
+                def backward(ctx, grad_loss):
+                    images, targets = ctx.saved_tensors
+                    grad = torch.empty_like(images)
+                    scale = grad_loss.detach().to(torch.float32).contiguous()
+                    check(_lib.load().spl_l2_image_loss_backward(_ptr(images), _ptr(targets), images.numel() // 4,
+                                                                 _ptr(scale), _ptr(grad), _stream_ptr(None)))
+                    return grad, None
+
+            cls.fn = L2ImageLoss
+        return cls.fn
+
+
+def l2_image_loss(images, targets):
+    """sum over pixels and RGB of (images[..., :3] - targets)^2 for float4 frames (..., 4) (r, g, b, T),
+    such as render_raw_views returns, against float32 RGB targets (..., 3): the value of
+    ((images[..., :3] - targets) ** 2).sum() (summed in another order) with the same gradient bit for
+    bit, (2 (image - target) * upstream, 0), each way in one pass over the frames."""
+    if images.dim() < 1 or images.shape[-1] != 4 or targets.shape[-1] != 3 or images.shape[:-1] != targets.shape[:-1]:
+        raise ValueError("l2_image_loss: images (..., 4) and targets (..., 3) with the same leading shape expected")
+    if images.dtype.itemsize != 4 or targets.dtype.itemsize != 4 or not images.is_cuda or not targets.is_cuda:
+        raise ValueError("l2_image_loss: float32 CUDA tensors expected")
+    return _L2ImageLoss.get().apply(images, targets)

@@ -1106,6 +1106,28 @@ int spl_activate_splats(uint64_t n, const float* means, const float* quaternions
     return SPL_OK;
 }
 
+uint32_t spl_l2_image_loss_partials(uint64_t pixels) { return l2_loss_partials(pixels); }
+
+int spl_l2_image_loss(const float* image, const float* target, uint64_t pixels, float* partial, void* stream) {
+    if (!image || !target || !partial) return fail(SPL_ERR_INVALID, "NULL argument");
+    if (reinterpret_cast<uintptr_t>(image) & 15u) return fail(SPL_ERR_INVALID, "image must be 16-byte aligned");
+    if (pixels == 0) return SPL_OK;
+    launch_l2_loss(image, target, pixels, partial, (cudaStream_t)stream);
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
+int spl_l2_image_loss_backward(const float* image, const float* target, uint64_t pixels, const float* scale_device,
+                               float* grad_image, void* stream) {
+    if (!image || !target || !scale_device || !grad_image) return fail(SPL_ERR_INVALID, "NULL argument");
+    if ((reinterpret_cast<uintptr_t>(image) | reinterpret_cast<uintptr_t>(grad_image)) & 15u)
+        return fail(SPL_ERR_INVALID, "image and grad_image must be 16-byte aligned");
+    if (pixels == 0) return SPL_OK;
+    launch_l2_loss_backward(image, target, pixels, scale_device, grad_image, (cudaStream_t)stream);
+    CU(cudaGetLastError());
+    return SPL_OK;
+}
+
 int spl_activate_splats_backward(uint64_t n, const float* quaternions, const float* log_scales, const float* rotation,
                                  const float* scale_alpha, const float* grad_x, const float* grad_y,
                                  const float* grad_z, const float* grad_rotation, const float* grad_scale_alpha,

@@ -3,6 +3,8 @@
 //                        arrays (x, y, z planes, unit rotations, scale + opacity), with the exact
 //                        arithmetic of Scene::load_chunk (scene.rs:225-250; activate_splat)
 //   k_activate_backward  gradients of the scene's arrays -> gradients of the raw parameters
+//   k_l2_loss            the L2 image loss of float4 frames against RGB targets (block partial sums)
+//   k_l2_loss_backward   its gradient, 2 (image - target) times the upstream gradient, in one pass
 #include "spl_device.cuh"
 
 namespace spl {
@@ -63,6 +65,45 @@ __global__ void __launch_bounds__(256) k_activate_backward(
     }
 }
 
+// sum over pixels and RGB of (image - target)^2; image: float4 (r, g, b, T) per pixel, target: three
+// floats per pixel.  Each block writes its partial sum to partial[blockIdx.x].
+__global__ void __launch_bounds__(256) k_l2_loss(const float4* __restrict__ image, const float* __restrict__ target,
+                                                 uint64_t pixels, float* __restrict__ partial) {
+    __shared__ float s_w[8];
+    float acc = 0.0f;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * (uint64_t)blockDim.x) {
+        const float4 c = __ldg(image + p);
+        const float* t = target + 3 * p;
+        const float dr = c.x - __ldg(t), dg = c.y - __ldg(t + 1), db = c.z - __ldg(t + 2);
+        acc += (dr * dr + dg * dg) + db * db;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, o);
+    if ((threadIdx.x & 31u) == 0u) s_w[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sum = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) sum += s_w[w];
+        partial[blockIdx.x] = sum;
+    }
+}
+
+// grad = (2 (image - target) * scale, 0) per pixel, scale read from device memory (the upstream
+// gradient of the loss, with no host round trip): the products torch's autograd forms for the same
+// expression, so the result is the same bit for bit.
+__global__ void __launch_bounds__(256) k_l2_loss_backward(const float4* __restrict__ image,
+                                                          const float* __restrict__ target, uint64_t pixels,
+                                                          const float* __restrict__ scale, float4* __restrict__ grad) {
+    const float sc = __ldg(scale);
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * (uint64_t)blockDim.x) {
+        const float4 c = __ldg(image + p);
+        const float* t = target + 3 * p;
+        const float dr = c.x - __ldg(t), dg = c.y - __ldg(t + 1), db = c.z - __ldg(t + 2);
+        grad[p] = make_float4(sc * (2.0f * dr), sc * (2.0f * dg), sc * (2.0f * db), 0.0f);
+    }
+}
+
 static uint32_t grid_for(uint64_t n) {
     const uint64_t b = (n + 255) / 256, cap = (uint64_t)device_sm_count() * 16u;
     return (uint32_t)(b < cap ? (b ? b : 1) : cap);
@@ -73,6 +114,18 @@ void launch_activate(uint32_t n, const float* means, const float* quats, const f
     if (n == 0) return;
     k_activate<<<grid_for(n), 256, 0, st>>>(n, means, reinterpret_cast<const float4*>(quats), logs, logits, x, y, z,
                                              reinterpret_cast<float4*>(rot), reinterpret_cast<float4*>(scale_alpha));
+}
+
+uint32_t l2_loss_partials(uint64_t pixels) { return grid_for(pixels); }
+
+void launch_l2_loss(const float* image, const float* target, uint64_t pixels, float* partial, cudaStream_t st) {
+    k_l2_loss<<<grid_for(pixels), 256, 0, st>>>(reinterpret_cast<const float4*>(image), target, pixels, partial);
+}
+
+void launch_l2_loss_backward(const float* image, const float* target, uint64_t pixels, const float* scale,
+                             float* grad, cudaStream_t st) {
+    k_l2_loss_backward<<<grid_for(pixels), 256, 0, st>>>(reinterpret_cast<const float4*>(image), target, pixels, scale,
+                                                         reinterpret_cast<float4*>(grad));
 }
 
 void launch_activate_backward(uint32_t n, const float* quats, const float* logs, const float* rot,

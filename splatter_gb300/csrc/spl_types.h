@@ -125,6 +125,12 @@ void launch_activate_backward(uint32_t n, const float* quats, const float* logs,
                               const float* scale_alpha, const float* gx, const float* gy, const float* gz,
                               const float* grot, const float* gsa, float* g_means, float* g_quats, float* g_logs,
                               float* g_logits, cudaStream_t st);
+// The L2 image loss of float4 frames against RGB targets (k_activate.cu): l2_loss_partials(pixels)
+// block partial sums, and its gradient (2 (image - target) * *scale, 0).
+uint32_t l2_loss_partials(uint64_t pixels);
+void launch_l2_loss(const float* image, const float* target, uint64_t pixels, float* partial, cudaStream_t st);
+void launch_l2_loss_backward(const float* image, const float* target, uint64_t pixels, const float* scale,
+                             float* grad, cudaStream_t st);
 // Backward of the last frame (fp32 blend): raster backward into grad_rec (10 floats per record),
 // then the vertex-stage backward into per-splat parameter gradients.  deferred: 1 + max_n words (the
 // needles and discs whose vertex-stage sweep runs in double).

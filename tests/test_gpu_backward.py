@@ -361,6 +361,27 @@ def test_backward_rejects_unaligned_gradient_arrays(cuda):
     assert float(aligned[2].abs().sum()) > 0.0  # SH gradients were written
 
 
+def test_l2_image_loss_equals_torch(cuda):
+    """l2_image_loss against the torch expression it replaces, ((images[..., :3] - targets) ** 2).sum():
+    the same loss to summation rounding and the same gradient bit for bit, with a non-unit upstream
+    gradient and a pixel count that is not a multiple of the block size."""
+    import torch
+    from splatter_gb300.autograd import l2_image_loss
+    g = torch.Generator(device="cuda").manual_seed(5)
+    images = torch.rand((3, 37, 53, 4), device="cuda", generator=g)
+    targets = torch.rand((3, 37, 53, 3), device="cuda", generator=g)
+    a = images.clone().requires_grad_(True)
+    b = images.clone().requires_grad_(True)
+    la = l2_image_loss(a, targets)
+    lb = ((b[..., :3] - targets) ** 2).sum()
+    (la * 0.37).backward()
+    (lb * 0.37).backward()
+    assert torch.allclose(la, lb, rtol=1e-6, atol=0.0)
+    assert torch.equal(a.grad, b.grad)
+    with pytest.raises(ValueError):
+        l2_image_loss(images[..., :3], targets)
+
+
 def test_render_raw_views_equals_per_view_sum(cuda):
     """render_raw_views: the stacked frames equal render_raw's frame of each view bit for bit, and
     the in-place accumulated gradients equal the per-view render_raw gradients that autograd sums

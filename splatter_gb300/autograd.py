@@ -365,6 +365,7 @@ def l2_image_loss(images, targets):
     bit, (2 (image - target) * upstream, 0), each way in one pass over the frames."""
     if images.dim() < 1 or images.shape[-1] != 4 or targets.shape[-1] != 3 or images.shape[:-1] != targets.shape[:-1]:
         raise ValueError("l2_image_loss: images (..., 4) and targets (..., 3) with the same leading shape expected")
-    if images.dtype.itemsize != 4 or targets.dtype.itemsize != 4 or not images.is_cuda or not targets.is_cuda:
+    torch = _import_torch()
+    if images.dtype != torch.float32 or targets.dtype != torch.float32 or not images.is_cuda or not targets.is_cuda:
         raise ValueError("l2_image_loss: float32 CUDA tensors expected")
     return _L2ImageLoss.get().apply(images, targets)

@@ -8,7 +8,8 @@ Renderer with the cooperative sort.
 import numpy as np
 import pytest
 
-from splatter_gb300 import SORT_ONESWEEP, Configuration, Renderer, Scene, SplatterError, camera, synthetic
+from splatter_gb300 import (SORT_ONESWEEP, BlendMode, Configuration, DepthSorting, Renderer, Scene, SplatterError,
+                             camera, synthetic)
 
 pytestmark = pytest.mark.gpu
 
@@ -96,6 +97,45 @@ def test_render_frame_replays_its_own_graph(cuda):
         kb, ib, _ = direct.sorted_entries()
         assert torch.equal(ka, kb) and torch.equal(ia, ib)
     assert int((want[..., 3] != 255).sum()) > 1000  # something drawn
+
+
+GRAPH_MODES = [
+    dict(depth_sorting=DepthSorting.NONE),
+    dict(depth_sorting=DepthSorting.CPU),
+    dict(depth_sorting=DepthSorting.GPU_INDIRECT_DRAW),
+    dict(depth_sorting=DepthSorting.GPU, use_unaligned_rectangles=False, use_covariance_for_scale=False),
+    dict(depth_sorting=DepthSorting.GPU, blend_mode=BlendMode.FP32, spherical_harmonics_order=1),
+]
+
+
+@pytest.mark.parametrize("mode", GRAPH_MODES, ids=lambda m: "-".join(f"{k}={int(v)}" for k, v in m.items()))
+@pytest.mark.parametrize("sort_mode", ["cooperative", "onesweep"])
+def test_own_graph_replay_in_every_mode(cuda, mode, sort_mode):
+    """The renderer's own frame graph (captured on the second frame of a viewport and scene size,
+    replayed after) in the other depth-sorting modes, rectangle kinds, semi-axis methods and blend
+    targets, with either sort: every frame equals a renderer's direct launches bit for bit."""
+    import torch
+    n, W, H = 40000, 320, 240
+    cfg = Configuration(max_splat_count=n, **{"spherical_harmonics_order": 3, **mode})
+    rec = synthetic.clustered(n, seed=9, sh_order=3)
+    poses = camera.orbit_poses(6, seed=10, radius=(6.0, 14.0))
+    direct = Renderer(cfg)
+    direct.set_frame_graphs(False)
+    r = Renderer(cfg)
+    if sort_mode == "onesweep":
+        direct.set_sort_mode(SORT_ONESWEEP)
+        r.set_sort_mode(SORT_ONESWEEP)
+    sd, sr = _scene_on(direct, rec), _scene_on(r, rec)
+    drawn = 0
+    for k, pose in enumerate(poses):
+        want = direct.render_frame(sd, pose, W, H).cpu()
+        got = r.render_frame(sr, pose, W, H).cpu()
+        torch.cuda.synchronize()
+        assert torch.equal(got, want), f"frame {k}"
+        a, b = r.frame_info(), direct.frame_info()
+        assert (a.visible_count, a.draw_count, a.pair_count) == (b.visible_count, b.draw_count, b.pair_count)
+        drawn = max(drawn, a.pair_count)
+    assert drawn > 1000
 
 
 def _scene_on(renderer, rec):

@@ -256,6 +256,56 @@ def test_parameter_gradients_match_finite_differences(frame):
         assert np.mean(rel_fd[agree] <= REL_TOL) >= 0.99
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["none", "cpu-keys", "gpu", "gpu-indirect"])
+def test_backward_in_other_depth_sorting_modes(cuda, mode):
+    """The backward re-walks each tile in the frame's draw order: index order without sorting, the
+    reference's CPU keys, or the indirect draw's order.  Every parameter of every drawn splat against
+    the FP64 reference gradient of the same mode (the oracle's draw list for it): >= 99.8% within 1e-3
+    of max(|ref|, floor), splats at FP32/FP64 decision boundaries excluded (the default mode measures
+    99.86% on this scene of large splats), and far fewer against another mode's draw order."""
+    import torch
+    from splatter_gb300 import DepthSorting
+    n, W, H = 5000, 160, 120
+    rec = synthetic.plain_small(n, seed=83, sh_order=3)
+    rec[:, 55:58] += 1.0
+    cam = camera.look_at([0.3, 0.5, -7.0], [0.0, 0.0, 0.0])
+    cfg = Configuration(max_splat_count=n, spherical_harmonics_order=3, blend_mode=BlendMode.FP32,
+                        field_of_view_y=math.radians(60), depth_sorting=DepthSorting(mode))
+    r = Renderer(cfg)
+    seed_sc = oracle.load_transform(rec)
+    t = [torch.tensor(a, device="cuda") for a in (np.ascontiguousarray(seed_sc["center"].T), seed_sc["rotation"],
+                                                 np.concatenate([seed_sc["scale"], seed_sc["alpha"][:, None]], 1),
+                                                 seed_sc["sh"])]
+    target = render_splats(*t, r, cam, W, H)[..., :3].cpu().numpy().astype(np.float64)
+    sc = oracle.load_transform(_perturbed(rec, seed=84))
+    loss, g, img = _gpu_grads(r, sc, cam, W, H, target)
+    u = oracle.uniforms(cam, W, H, fovy=cfg.field_of_view_y)
+    ocfg = oracle.config_struct(depth_sorting=mode, sh_order=3, blend_mode=1)
+    refs = {}
+    for m in (mode, 0 if mode != 0 else 2):  # this mode, and another draw order for contrast
+        ctx = oracle.GradContext(u, oracle.config_struct(depth_sorting=m, sh_order=3, blend_mode=1),
+                                 {k: v.astype(np.float64) for k, v in sc.items()}, target)
+        try:
+            loss64, ref, _ = ctx.loss_and_grad(threads=16)
+            amb, _ = ctx.ambiguous(threads=16)
+        finally:
+            ctx.close()
+        refs[m] = (loss64, ref, amb)
+    loss64, ref, amb = refs[mode]
+    assert abs(loss - loss64) <= 1e-3 * loss64
+    drawn_all = np.nonzero(np.abs(ref).sum(1) > 0)[0]
+    drawn = drawn_all[~amb[drawn_all]]
+    assert len(drawn) > 500 and len(drawn) >= 0.9 * len(drawn_all)
+    idx = [(k, p) for k in drawn for p in range(59)]
+    rel, floor = _compare(g, ref, idx)
+    other = [m for m in refs if m != mode][0]
+    rel_other, _ = _compare(g, refs[other][1], idx)
+    print(f"mode {mode}: {len(drawn)} drawn splats, {100 * np.mean(rel <= REL_TOL):.3f}% within {REL_TOL} "
+          f"of its FP64 reference, {100 * np.mean(rel_other <= REL_TOL):.3f}% of mode {other}'s")
+    assert np.mean(rel <= REL_TOL) >= 0.998
+    assert np.mean(rel_other <= REL_TOL) < 0.5  # measured ~5%: the order decides the gradients
+
+
 def test_raw_parameter_gradients_through_autograd(cuda):
     """render_raw: the loader's activations and their backward on the GPU around the hand-written
     backward.  The frame equals the frame of a scene loaded from the same file records, and the raw

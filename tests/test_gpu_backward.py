@@ -256,20 +256,17 @@ def test_parameter_gradients_match_finite_differences(frame):
         assert np.mean(rel_fd[agree] <= REL_TOL) >= 0.99
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["none", "cpu-keys", "gpu", "gpu-indirect"])
-def test_backward_in_other_depth_sorting_modes(cuda, mode):
-    """The backward re-walks each tile in the frame's draw order: index order without sorting, the
-    reference's CPU keys, or the indirect draw's order.  Every parameter of every drawn splat against
-    the FP64 reference gradient of the same mode (the oracle's draw list for it): >= 99.8% within 1e-3
-    of max(|ref|, floor), splats at FP32/FP64 decision boundaries excluded (the default mode measures
-    99.86% on this scene of large splats), and far fewer against another mode's draw order."""
+def _small_frame_against_fp64(mode, sh_order, contrast):
+    """5000 splats at 160x120 in a depth-sorting mode and SH degree: the GPU's parameter gradients and
+    their agreement with the FP64 reference gradient of the same mode (and, with `contrast`, of
+    another mode's draw order)."""
     import torch
     from splatter_gb300 import DepthSorting
     n, W, H = 5000, 160, 120
-    rec = synthetic.plain_small(n, seed=83, sh_order=3)
+    rec = synthetic.plain_small(n, seed=83, sh_order=sh_order)
     rec[:, 55:58] += 1.0
     cam = camera.look_at([0.3, 0.5, -7.0], [0.0, 0.0, 0.0])
-    cfg = Configuration(max_splat_count=n, spherical_harmonics_order=3, blend_mode=BlendMode.FP32,
+    cfg = Configuration(max_splat_count=n, spherical_harmonics_order=sh_order, blend_mode=BlendMode.FP32,
                         field_of_view_y=math.radians(60), depth_sorting=DepthSorting(mode))
     r = Renderer(cfg)
     seed_sc = oracle.load_transform(rec)
@@ -280,10 +277,9 @@ def test_backward_in_other_depth_sorting_modes(cuda, mode):
     sc = oracle.load_transform(_perturbed(rec, seed=84))
     loss, g, img = _gpu_grads(r, sc, cam, W, H, target)
     u = oracle.uniforms(cam, W, H, fovy=cfg.field_of_view_y)
-    ocfg = oracle.config_struct(depth_sorting=mode, sh_order=3, blend_mode=1)
     refs = {}
-    for m in (mode, 0 if mode != 0 else 2):  # this mode, and another draw order for contrast
-        ctx = oracle.GradContext(u, oracle.config_struct(depth_sorting=m, sh_order=3, blend_mode=1),
+    for m in ((mode, 0 if mode != 0 else 2) if contrast else (mode,)):
+        ctx = oracle.GradContext(u, oracle.config_struct(depth_sorting=m, sh_order=sh_order, blend_mode=1),
                                  {k: v.astype(np.float64) for k, v in sc.items()}, target)
         try:
             loss64, ref, _ = ctx.loss_and_grad(threads=16)
@@ -296,14 +292,43 @@ def test_backward_in_other_depth_sorting_modes(cuda, mode):
     drawn_all = np.nonzero(np.abs(ref).sum(1) > 0)[0]
     drawn = drawn_all[~amb[drawn_all]]
     assert len(drawn) > 500 and len(drawn) >= 0.9 * len(drawn_all)
-    idx = [(k, p) for k in drawn for p in range(59)]
-    rel, floor = _compare(g, ref, idx)
-    other = [m for m in refs if m != mode][0]
-    rel_other, _ = _compare(g, refs[other][1], idx)
-    print(f"mode {mode}: {len(drawn)} drawn splats, {100 * np.mean(rel <= REL_TOL):.3f}% within {REL_TOL} "
-          f"of its FP64 reference, {100 * np.mean(rel_other <= REL_TOL):.3f}% of mode {other}'s")
-    assert np.mean(rel <= REL_TOL) >= 0.998
-    assert np.mean(rel_other <= REL_TOL) < 0.5  # measured ~5%: the order decides the gradients
+    nparam = 11 + 3 * (sh_order + 1) ** 2
+    idx = [(k, p) for k in drawn for p in range(nparam)]
+    rel, _ = _compare(g, ref, idx)
+    geo = np.array([p < 11 for k, p in idx])
+    frac_geo, frac_sh = float(np.mean(rel[geo] <= REL_TOL)), float(np.mean(rel[~geo] <= REL_TOL))
+    frac_other = None
+    if contrast:
+        other = [m for m in refs if m != mode][0]
+        rel_other, _ = _compare(g, refs[other][1], idx)
+        frac_other = float(np.mean(rel_other <= REL_TOL))
+    print(f"mode {mode}, SH {sh_order}: {len(drawn)} drawn splats within {REL_TOL} of the FP64 reference: "
+          f"centre/rotation/scale/opacity {100 * frac_geo:.3f}%, SH {100 * frac_sh:.3f}%"
+          + ("" if frac_other is None else f"; {100 * frac_other:.3f}% of all against another mode's order"))
+    return frac_geo, frac_sh, frac_other
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["none", "cpu-keys", "gpu", "gpu-indirect"])
+def test_backward_in_every_depth_sorting_mode(cuda, mode):
+    """The backward re-walks each tile in the frame's draw order: index order without sorting, the
+    reference's CPU keys, the GPU keys or the indirect draw's order.  Every parameter of every drawn
+    splat against the FP64 reference gradient of the same mode (the oracle's draw list for it), within
+    1e-3 of max(|ref|, floor), splats at FP32/FP64 decision boundaries excluded: >= 99% of the centre,
+    rotation, scale and opacity gradients (99.16-99.28% measured on this scene of large splats, where
+    the sums over a splat's pixels cancel more than at 20k splats) and >= 99.95% of the SH gradients;
+    against another mode's draw order ~5% of all (the order decides the gradients)."""
+    frac_geo, frac_sh, frac_other = _small_frame_against_fp64(mode, 3, contrast=True)
+    assert frac_geo >= 0.99 and frac_sh >= 0.9995
+    assert frac_other < 0.5
+
+
+@pytest.mark.parametrize("sh_order", [0, 1, 2])
+def test_backward_at_lower_sh_degrees(cuda, sh_order):
+    """The vertex-stage backward is compiled per SH degree: degrees 0-2 against the FP64 reference
+    gradient of the same degree, with the bars of the depth-sorting test (99.29-99.40% and >= 99.99%
+    measured)."""
+    frac_geo, frac_sh, _ = _small_frame_against_fp64(2, sh_order, contrast=False)
+    assert frac_geo >= 0.99 and frac_sh >= 0.9995
 
 
 def test_raw_parameter_gradients_through_autograd(cuda):

@@ -15,7 +15,7 @@ import pytest
 import oracle
 from splatter_gb300 import BlendMode, Configuration, DepthSorting, Renderer, Scene, SplatterError, camera, synthetic
 from splatter_gb300 import _lib
-from tests.helpers import default_cam, image_psnr, oracle_cfg, oracle_uniforms, scene_from_splats60
+from tests.helpers import default_cam, image_psnr, oracle_cfg, oracle_uniforms
 
 pytestmark = pytest.mark.gpu
 

@@ -331,6 +331,26 @@ def test_depth_key_layout():
     assert xb > 255 and (keys[3] >> 8) & 0x1FF == (xb & 0x1FF) | ((keys[3] >> 8) & 0x100)
 
 
+@pytest.mark.parametrize("mode", [1, 2], ids=["cpu-rule", "gpu-rule"])
+def test_frustum_boundaries(mode):
+    # isInFrustum (shaders.wgsl:54-61; renderer.rs:381-387 for the CPU rule): visible iff |x| < tol,
+    # |y| < tol and |z - 0.5| < 0.5 in normalised device coordinates.  A 90-degree square view from the
+    # origin along +z maps (x, y, z) to (x / z, y / z) and depth (1000/999)(1 - 1/z): the near plane is
+    # view z = 1 and the far plane z = 1000.  Points 1e-4 (relative) inside and outside every bound.
+    cam = camera.look_at([0.0, 0.0, 0.0], [0.0, 0.0, 1.0])
+    u = oracle.uniforms(cam, 100, 100, tol=1.1)
+    e = 1e-4
+    cases = [((11 * (1 - e), 0, 10), True), ((11 * (1 + e), 0, 10), False),
+             ((-11 * (1 - e), 0, 10), True), ((-11 * (1 + e), 0, 10), False),
+             ((0, 11 * (1 - e), 10), True), ((0, 11 * (1 + e), 10), False),
+             ((0, -11 * (1 - e), 10), True), ((0, -11 * (1 + e), 10), False),
+             ((0, 0, 1 + 1e-3), True), ((0, 0, 1 - 1e-3), False),
+             ((0, 0, 999), True), ((0, 0, 1001), False), ((0, 0, -5), False), ((0, 0, 0), False)]
+    pts = np.array([c[0] for c in cases], np.float32)
+    _, vis = oracle.cull_keys(u, mode, pts)
+    assert vis.tolist() == [c[1] for c in cases]
+
+
 def test_cpu_rule_and_fallback_sort_stable():
     rng = np.random.default_rng(5)
     pts = rng.normal(0, 2, (5000, 3)).astype(np.float32)

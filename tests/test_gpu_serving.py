@@ -218,6 +218,36 @@ def test_server_one_slot_is_the_plain_loop(cuda, alone):
     srv.close()
 
 
+@pytest.mark.parametrize("graphs", [True, False], ids=["graphs", "direct"])
+def test_served_fp32_square_frames_equal_alone(cuda, graphs):
+    """The FP32 blend target (float4 pixels) with axis-aligned squares and ellipse-equation semi-axes:
+    served frames (four slots, a budget that forces evictions) equal the same frames rendered alone,
+    bit for bit."""
+    import torch
+    from splatter_gb300.serving import Server
+    cfg = Configuration(max_splat_count=max(SIZES), spherical_harmonics_order=2, blend_mode=BlendMode.FP32,
+                        use_unaligned_rectangles=False, use_covariance_for_scale=False)
+    scenes = [synthetic.clustered(n, seed=30 + i, sh_order=3) for i, n in enumerate(SIZES)]
+    reqs = _requests(20, seed=31)
+    r = Renderer(cfg)
+    objs = [_scene_on(r, rec) for rec in scenes]
+    want = [r.render_frame(objs[sid], pose, w, h).cpu() for sid, pose, (w, h) in reqs]
+    torch.cuda.synchronize()
+    srv = Server(cfg, slots=4, use_graphs=graphs, scene_memory_budget=40 << 20, max_width=480, max_height=270)
+    for rec in scenes:
+        srv.add_scene(rec)
+    outs = [srv.output_buffer(w, h) for _, _, (w, h) in reqs]
+    assert all(o.dtype == torch.float32 for o in outs)
+    for (sid, pose, (w, h)), out in zip(reqs, outs):
+        srv.submit(sid, pose, w, h, out)
+    done = srv.wait_all(len(reqs))
+    assert all(c.status == 0 for c in done)
+    for out, im in zip(outs, want):
+        assert torch.equal(out.view(torch.int32), im.view(torch.int32))
+    assert srv.stats()["restores"] > 0
+    srv.close()
+
+
 def test_server_rejects_bad_requests(cuda):
     from splatter_gb300.serving import Server
     srv = Server(_cfg(50000), slots=2, max_width=128, max_height=128)

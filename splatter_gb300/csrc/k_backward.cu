@@ -292,7 +292,7 @@ __device__ __forceinline__ void store_splat_gradient(uint32_t i, const float* gi
 // Float sweep of every drawn splat but the needles and discs (needs_double_sweep), whose slots go to
 // `deferred` ([0] the count, then the slots) for k_preprocess_backward_double; SH gradients of all.
 template <int SHO, bool COV>
-__global__ void __launch_bounds__(128, 3) k_preprocess_backward(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
+__global__ void __launch_bounds__(128, 4) k_preprocess_backward(SceneView s, Uniforms u, const uint32_t* __restrict__ idx,
                                                              const FrameCounters* __restrict__ fc,
                                                              const uint2* __restrict__ boxes,
                                                              const float* __restrict__ grad_rec, float* gx, float* gy,
